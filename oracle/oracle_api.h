@@ -1,0 +1,61 @@
+/* C interface of the CPU oracle (test infrastructure; see tracer_oracle.cpp).
+ * Scene arrays use the same std430 records as the product's C ABI. */
+#ifndef ORACLE_API_H
+#define ORACLE_API_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_scene {
+    const float* triangles;       /* 48 B records; v0.w lane = material id (u32) */
+    uint32_t num_triangles;
+    const float* materials;       /* 48 B records */
+    uint32_t num_materials;
+    const float* spheres;         /* 64 B records (Material + centre + radius) */
+    uint32_t num_spheres;
+    const float* planes;          /* 64 B records (Material + normal + offset) */
+    uint32_t num_planes;
+    const void* tri_nodes;        /* 32 B BVH nodes over triangles, or NULL = linear scan */
+    uint32_t num_tri_nodes;
+    const uint32_t* tri_prim_index;
+    const void* sphere_nodes;     /* 32 B BVH nodes over spheres, or NULL */
+    uint32_t num_sphere_nodes;
+    const uint32_t* sphere_prim_index;
+} oracle_scene;
+
+typedef struct oracle_params {
+    uint32_t width, height, spp, max_depth, rr_start;
+    float sky[3];
+    int32_t tie_mode;   /* 0 = reference ties (linear scan), 1 = strict */
+    int32_t trig_mode;  /* 0 = portable cos/sin (rng_trig.h), 1 = libm */
+    int32_t threads;    /* 0 = all OpenMP threads */
+    uint32_t row_begin, row_end, row_step;  /* scanline subset; row_end 0 = height */
+} oracle_params;
+
+typedef struct oracle_stats {
+    uint64_t closest_rays, shadow_rays, node_fetches, tri_tests, sphere_tests, plane_tests, hits;
+} oracle_stats;
+
+int oracle_render(const oracle_scene* scene, const float* frame96, const oracle_params* params, float* rgba32f,
+                  uint8_t* rgba8, uint32_t* hit_id, float* hit_t, oracle_stats* stats);
+int oracle_render_f64(const oracle_scene* scene, const float* frame96, const oracle_params* params, float* rgba32f,
+                      double* accum, oracle_stats* stats);
+void oracle_rand(float cx, float cy, float salt, int trig_mode, int n, float* out);
+float oracle_cos(float x);
+float oracle_sin(float x);
+float oracle_tri_intersect(const float* o, const float* d, const float* tri48);
+float oracle_sphere_intersect(const float* o, const float* d, const float* c, float radius);
+float oracle_plane_intersect(const float* o, const float* d, const float* n, float len);
+int oracle_trace_ray(const oracle_scene* scene, int tie_mode, int shadow, const float* o, const float* d, float tmax,
+                     float* out, oracle_stats* stats);
+void oracle_radiance(const oracle_scene* scene, const float* frame96, const oracle_params* params, const float* o,
+                     const float* d, float cx, float cy, float salt, float* out_rgb, float* out_salt);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
