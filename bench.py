@@ -1,0 +1,319 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 path tracer (forward trace).
+
+Workload (the largest single-GPU configuration of the headline metric):
+c1 -- 1920x1080, 16 spp, max depth 8, Russian roulette from depth 3, a
+100k-triangle soup (centroids U[-50,50]^3, vertices + N(0, 0.5^2)), 256
+materials, 16-bin SAH BVH with leaf size 4, sky 1.0, seed 1.  Synthetic data.
+
+A step is one trace of the full frame.  `value` is Mrays/s with the scene
+resident in HBM (one ray = one trace_ray call, closest-hit or shadow, counted
+on the device); `e2e` is the same metric through the public C ABI with host
+buffers (FrameData in, RGBA8 image out to pinned host memory) inside the timed
+region.  L2 is flushed (256 MiB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: one process per GPU (torchrun); every rank traces its own frame
+(independent seeds), so per-GPU work is fixed: weak scaling, no data-path
+collective.  --impl reference times the CPU restatement of the reference
+shader (oracle/, with the same BVH) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "vk-renderer_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "Mrays/s on 1 GB300 (fwd, adjoint, batched) at ≤1e-3 RMSE vs plain trace"
+UNIT = "Mrays/s"
+L2_FLUSH_BYTES = 256 << 20
+
+# Per-launch DRAM traffic of k_persistent on this workload, from
+# profiles/k_persistent_c1.md (ncu dram__bytes_read.sum + dram__bytes_write.sum);
+# None until captured.
+NCU_TRAFFIC_BYTES = None
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.flush()
+        with open(self.f.name) as fh:
+            rows = [r.split(",") for r in fh.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for k, n in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(st: dict, pixels: int, out_bytes_per_pixel: int) -> int:
+    """Bytes one trace must read/write by definition: 32 B per BVH node record
+    fetched, 48 B per triangle and 64 B per sphere/plane tested, 48 B material
+    per closest hit, plus the image written."""
+    return (32 * st["node_fetches"] + 48 * st["tri_tests"] + 64 * st["sphere_tests"] + 64 * st["plane_tests"]
+            + 48 * st["hits"] + out_bytes_per_pixel * pixels)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline_sample(wl, tri_bvh, seconds_target: float = 15.0):
+    """Oracle (CPU port of the shader, same BVH) on a bounded row subset, all
+    host threads.  Returns (Mrays/s, threads, description)."""
+    import pyoracle
+    pyoracle.build()
+    threads = os.cpu_count() or 1
+    step = 64
+    rows = (0, wl.height, step)
+    prm = pyoracle.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start, sky=wl.sky,
+                          tie_mode=wl.tie_mode, trig_mode=0, threads=threads, rows=rows)
+    t0 = time.perf_counter()
+    out = pyoracle.render(wl.scene, wl.frame, prm, tri_bvh=tri_bvh)
+    dt = time.perf_counter() - t0
+    # grow the sample toward the target duration
+    if dt < seconds_target / 4:
+        step = max(1, int(step * dt / (seconds_target / 2)) or 1)
+        prm = pyoracle.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                              sky=wl.sky, tie_mode=wl.tie_mode, trig_mode=0, threads=threads, rows=(0, wl.height, step))
+        t0 = time.perf_counter()
+        out = pyoracle.render(wl.scene, wl.frame, prm, tri_bvh=tri_bvh)
+        dt = time.perf_counter() - t0
+    st = out["stats"]
+    rays = st["closest_rays"] + st["shadow_rays"]
+    nrows = len(range(0, wl.height, step))
+    return rays / dt / 1e6, threads, f"every {step}th scanline ({nrows} of {wl.height} rows, full width, " \
+                                     f"{wl.spp} spp), {dt:.1f} s, {rays} rays"
+
+
+def run_reference(args):
+    """CPU restatement of the reference shader (oracle port, same BVH), timed
+    on the host cores.  Rank 0 alone works under torchrun."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    from vktrace import abi, configs
+    import pyoracle
+    pyoracle.build()
+    wl = configs.c1()
+    nodes, idx, _ = abi.build_bvh(2, wl.scene.triangles, leaf_size=4, sah_bins=16)
+    threads = os.cpu_count() or 1
+    step = 128
+    times, rays_tot = [], 0
+    for k in range(args.warmup + args.steps):
+        prm = pyoracle.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                              sky=wl.sky, tie_mode=1, trig_mode=0, threads=threads,
+                              rows=((k * 7) % step, wl.height, step))
+        t0 = time.perf_counter()
+        out = pyoracle.render(wl.scene, wl.frame, prm, tri_bvh=(nodes, idx))
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            rays_tot += out["stats"]["closest_rays"] + out["stats"]["shadow_rays"]
+    total = sum(times)
+    value = rays_tot / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "spp": wl.spp,
+                   "max_depth": wl.max_depth, "rr_start": wl.rr_start, "triangles": len(wl.scene.triangles),
+                   "bvh": "sah16-leaf4", "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step: every {step}th scanline of the frame (offset varies), full width, "
+                                   f"{wl.spp} spp; CPU restatement of Tracer.comp with the same BVH"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from vktrace import abi, configs
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    wl = configs.c1()
+    # weak scaling: each rank its own frame (different seed)
+    wl.frame["seed"] = np.float32(float(wl.frame["seed"]) + 0.125 * rank)
+    nodes, idx, bvh_depth = abi.build_bvh(2, wl.scene.triangles, leaf_size=4, sah_bins=16)
+    tr = abi.Tracer(local)
+    tr.upload_scene(wl.scene, tri_bvh=(nodes, idx))
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    kern = abi.KERNEL_PERSISTENT if args.kernel == "persistent" else abi.KERNEL_PLAIN
+    common = dict(spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start, sky=wl.sky, kernel=kern,
+                  block=args.block, wavefront=args.wavefront)
+    p_count = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=True, **common)
+    p_run = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=False, **common)
+    # counting pass (untimed): the kernel is deterministic, every step does this work
+    tr.trace(wl.frame, p_count, sptr)
+    st = tr.stats()
+    rays = st["closest_rays"] + st["shadow_rays"]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        tr.trace(wl.frame, p_run, sptr)
+    tr.synchronize()
+    torch.cuda.synchronize()
+
+    clk = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        evs[k][0].record(stream)
+        tr.trace(wl.frame, p_run, sptr)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    tr.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(step_ms) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * rays / (ms / 1e3) / 1e6
+
+    # end to end through the C ABI with host buffers
+    pinned = torch.empty((wl.height, wl.width, 4), dtype=torch.uint8, pin_memory=True)
+    img = pinned.numpy()
+    for _ in range(2):
+        tr.trace(wl.frame, p_run)
+        tr.readback(abi.AOV_RGBA8, img)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        tr.trace(wl.frame, p_run)
+        tr.readback(abi.AOV_RGBA8, img)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * rays / e2e_s / 1e6
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        ab = algorithmic_bytes(st, wl.pixels, 4)
+        achieved = ab / (ms / 1e3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "spp": wl.spp,
+                       "max_depth": wl.max_depth, "rr_start": wl.rr_start,
+                       "triangles": len(wl.scene.triangles), "materials": len(wl.scene.materials),
+                       "bvh": f"sah16-leaf4 depth {bvh_depth}", "kernel": args.kernel, "block": args.block,
+                       "l2": "flushed before each timed step (256 MiB write)",
+                       "parallelism": f"replica per GPU x{world} (independent frames)"},
+            "rays_per_step": rays,
+            "stats": st,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 96,
+                    "d2h_bytes_per_step": wl.pixels * 4},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
+                         "kernel": "k_persistent" if kern == abi.KERNEL_PERSISTENT else "k_plain",
+                         "algorithmic_bytes_per_launch": ab, "peak_source": peak_kind},
+            "clocks": clocks,
+            "gpu_launches": args.steps,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            v, cores, sample = cpu_baseline_sample(wl, (nodes, idx))
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        print(json.dumps(line), flush=True)
+    tr.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--kernel", choices=["persistent", "plain"], default="persistent")
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--wavefront", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

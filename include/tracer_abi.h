@@ -1,0 +1,251 @@
+/* tracer_abi.h - C ABI of the GB300 (sm_103a) path tracer.
+ *
+ * Drop-in for the compute dispatch of stickyfingies/vk-renderer:
+ *   Source/GraphicsDevice.cpp:796-822   scene SSBO creation and upload
+ *                                       -> tracer_upload_scene
+ *   Source/GraphicsDevice.cpp:986-1131  compute descriptors, pipeline,
+ *                                       96-byte push-constant range
+ *                                       -> tracer_create
+ *   Source/GraphicsDevice.cpp:1254-1266 bind + vkCmdPushConstants(FrameData)
+ *                                       + vkCmdDispatch(res/16, res/16, 1)
+ *                                       -> tracer_trace
+ *   Fullscreen.frag sampling the image  -> tracer_readback / tracer_device_image
+ * The kernel that runs is the CUDA restatement of Assets/Tracer.comp.
+ *
+ * Conventions: every call returns an int status (TRACER_OK = 0, errors < 0)
+ * and records a message for tracer_last_error.  Host pointers passed in are
+ * copied before the call returns; the caller keeps ownership.  A context is
+ * not thread-safe (the reference drives its device from one thread,
+ * Source/Main.cpp:148-196); separate contexts may be used from separate
+ * threads.  Structs below keep the reference's std430 layouts byte for byte.
+ */
+#ifndef TRACER_ABI_H
+#define TRACER_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes
+ * The first three mirror GraphicsDevice::Error (Include/GraphicsDevice.h:46-52),
+ * whose SUCCESS is TRACER_OK. */
+#define TRACER_OK 0
+#define TRACER_ERR_NO_SUITABLE_GPU (-1)     /* no CUDA device of the right kind */
+#define TRACER_ERR_NO_SUITABLE_SURFACE (-2) /* image size / AOV cannot be produced */
+#define TRACER_ERR_UNKNOWN (-3)
+#define TRACER_ERR_INVALID_ARG (-4)
+#define TRACER_ERR_OOM (-5)
+#define TRACER_ERR_TIMEOUT (-6)             /* a bounded wait for the GPU ran out */
+#define TRACER_ERR_TRAVERSAL_LIMIT (-7)     /* a ray exceeded the traversal step cap */
+#define TRACER_ERR_STACK_OVERFLOW (-8)      /* traversal stack too shallow for the BVH */
+#define TRACER_ERR_CUDA (-9)
+#define TRACER_ERR_NO_SCENE (-10)
+#define TRACER_ERR_BAD_BVH (-11)            /* BVH failed validation */
+
+/* ------------------------------------------------------------ std430 records */
+
+/* CameraData, Include/Camera.h:5-12 / struct Camera, Tracer.comp:22-35 (64 B) */
+typedef struct tracer_camera {
+    float pos[3];
+    float _pad0;
+    float dir[3];
+    float _pad1;
+    float right[3];
+    float _pad2;
+    float up[3];
+    float _pad3;
+} tracer_camera;
+
+/* FrameData push constants, Include/GraphicsDevice.h:20-29 /
+ * Tracer.comp:151-166 (96 B).  light_pos is carried but unused (deprecated in
+ * the shader, Tracer.comp:158-161). */
+typedef struct tracer_frame {
+    float aspect_ratio;
+    float seed;
+    float _pad0[2];
+    float light_pos[3];
+    float _pad1;
+    tracer_camera camera;
+} tracer_frame;
+
+#define TRACER_MAT_DIFFUSE 0u    /* Tracer.comp:51 */
+#define TRACER_MAT_DIELECTRIC 1u /* Tracer.comp:52; IOR read from roughness */
+
+/* struct Material, Tracer.comp:59-74 (48 B: albedo@0 emissive@16
+ * roughness@28 metalness@32 type@36) */
+typedef struct tracer_material {
+    float albedo[3];
+    uint32_t _pad0;
+    float emissive[3];
+    float roughness;
+    float metalness;
+    uint32_t type;
+    uint32_t _pad1[2];
+} tracer_material;
+
+/* struct Sphere, Tracer.comp:102-111 (64 B) */
+typedef struct tracer_sphere {
+    tracer_material mat;
+    float P[3];
+    float r;
+} tracer_sphere;
+
+/* struct Plane, Tracer.comp:118-125 (64 B) */
+typedef struct tracer_plane {
+    tracer_material mat;
+    float N[3];
+    float len;
+} tracer_plane;
+
+/* struct Triangle, Tracer.comp:127-132 / Include/GraphicsDevice.h:13-18
+ * (48 B).  The reference gives every triangle the constant material `mirror`
+ * (Tracer.comp:386); here v0's padding lane holds an index into the scene's
+ * material table, so a table whose entry 0 is `mirror` reproduces it. */
+typedef struct tracer_triangle {
+    float v0[3];
+    uint32_t material;
+    float v1[3];
+    uint32_t _pad1;
+    float v2[3];
+    uint32_t _pad2;
+} tracer_triangle;
+
+/* BVH node (32 B; the reference has no BVH).  count > 0: leaf holding
+ * primitives prim_index[left_or_first .. left_or_first + count); count == 0:
+ * interior node whose children are nodes left_or_first and left_or_first + 1.
+ * Node 0 is the root. */
+typedef struct tracer_bvh_node {
+    float bmin[3];
+    int32_t left_or_first;
+    float bmax[3];
+    int32_t count;
+} tracer_bvh_node;
+
+/* ------------------------------------------------------------ BVH building */
+#define TRACER_BVH_NONE 0   /* linear scan, as Tracer.comp:378-428 */
+#define TRACER_BVH_MEDIAN 1 /* median split on the longest centroid axis */
+#define TRACER_BVH_SAH 2    /* binned surface-area heuristic */
+
+#define TRACER_PRIM_TRIANGLE 0
+#define TRACER_PRIM_SPHERE 1
+
+/* Builds a BVH over n triangles (tracer_triangle) or spheres (tracer_sphere).
+ * nodes_out needs room for 2n - 1 nodes, prim_index_out for n entries.
+ * Node boxes are padded outward slightly so that floating-point rounding in
+ * traversal never culls a box whose primitive a ray hits.  Deterministic:
+ * the same input gives the same nodes on every host. */
+int tracer_build_bvh(int kind, int prim_type, const void* prims, uint32_t n, uint32_t leaf_size, uint32_t sah_bins,
+                     tracer_bvh_node* nodes_out, uint32_t* num_nodes_out, uint32_t* prim_index_out,
+                     uint32_t* depth_out);
+
+/* Checks a BVH: indices in range, every primitive referenced exactly once,
+ * each box contains its children's boxes and its primitives.  Returns
+ * TRACER_OK or TRACER_ERR_BAD_BVH; *depth_out gets the tree depth. */
+int tracer_validate_bvh(int prim_type, const void* prims, uint32_t n, const tracer_bvh_node* nodes,
+                        uint32_t num_nodes, const uint32_t* prim_index, uint32_t* depth_out);
+
+/* ------------------------------------------------------------ scene */
+typedef struct tracer_scene_desc {
+    const tracer_triangle* triangles;
+    uint32_t num_triangles;
+    const tracer_material* materials; /* table indexed by tracer_triangle.material */
+    uint32_t num_materials;
+    const tracer_sphere* spheres;
+    uint32_t num_spheres;
+    const tracer_plane* planes; /* always scanned linearly (unbounded) */
+    uint32_t num_planes;
+    int32_t bvh;        /* TRACER_BVH_*; NONE = linear scan of triangles and spheres */
+    uint32_t leaf_size; /* 0 = 2 (median) / 4 (SAH) */
+    uint32_t sah_bins;  /* 0 = 16 */
+    /* Optional prebuilt BVHs (validated on upload); NULL = build here. */
+    const tracer_bvh_node* tri_nodes;
+    uint32_t num_tri_nodes;
+    const uint32_t* tri_prim_index;
+    const tracer_bvh_node* sphere_nodes;
+    uint32_t num_sphere_nodes;
+    const uint32_t* sphere_prim_index;
+} tracer_scene_desc;
+
+/* ------------------------------------------------------------ tracing */
+#define TRACER_TIES_REFERENCE 0 /* Tracer.comp:382/:402/:418 scan-order rule; linear scan only */
+#define TRACER_TIES_STRICT 1    /* nearest (t, primitive id) below tmax; required with a BVH */
+
+#define TRACER_KERNEL_AUTO 0
+#define TRACER_KERNEL_PLAIN 1      /* one thread per pixel, nested sample/bounce loops */
+#define TRACER_KERNEL_PERSISTENT 2 /* persistent warps, per-lane pixel refill */
+
+#define TRACER_AOV_RGBA8 0       /* w*h*4 u8: what imageStore writes (Tracer.comp:592) */
+#define TRACER_AOV_RGBA32F 1     /* w*h*4 f32: the colour before UNORM8 conversion */
+#define TRACER_AOV_PRIMARY_HIT 2 /* w*h*(u32 prim id, f32 t) of the first ray of each pixel */
+#define TRACER_AOV_STATS 3       /* one tracer_stats */
+
+/* Primitive ids in PRIMARY_HIT: triangles 0..nt-1, spheres nt..nt+ns-1,
+ * planes after; 0xFFFFFFFF (and t = -1) on a miss. */
+
+typedef struct tracer_trace_params {
+    uint32_t width, height; /* storage-image size (RAYTRACE_RESOLUTION^2 in the reference) */
+    uint32_t spp;           /* SAMPLES, Tracer.comp:180 (reference 4) */
+    uint32_t max_depth;     /* DEPTH, Tracer.comp:179 (reference 4) */
+    uint32_t rr_start;      /* first depth with Russian roulette (reference 0: every depth) */
+    float sky[3];           /* radiance returned by a miss (reference 0) */
+    int32_t tie_mode;       /* TRACER_TIES_* */
+    int32_t kernel;         /* TRACER_KERNEL_* */
+    uint32_t block;         /* threads per block (multiple of 32, <= 1024); 0 = default */
+    uint32_t stack_depth;   /* traversal stack entries per thread; 0 = BVH depth */
+    uint32_t wavefront;     /* persistent kernel: resident CTAs per SM; 0 = occupancy maximum */
+    uint32_t aov_mask;      /* bit (1 << TRACER_AOV_*) per image written; 0 = RGBA8 only */
+    uint32_t stats;         /* nonzero: count rays, node fetches and primitive tests */
+} tracer_trace_params;
+
+typedef struct tracer_stats {
+    uint64_t closest_rays; /* trace_ray calls for the path (Tracer.comp:445) */
+    uint64_t shadow_rays;  /* trace_ray calls for next-event estimation (:473) */
+    uint64_t node_fetches; /* 32 B BVH node records read */
+    uint64_t tri_tests;    /* 48 B triangle records tested */
+    uint64_t sphere_tests; /* 64 B sphere records tested */
+    uint64_t plane_tests;  /* 64 B plane records tested */
+    uint64_t hits;         /* closest-hit rays that found a hit (each reads a 48 B material) */
+} tracer_stats;
+
+typedef struct tracer_ctx tracer_ctx;
+
+/* Replaces GraphicsDevice::Construct's compute set-up (GraphicsDevice.cpp:986-1131). */
+int tracer_create(tracer_ctx** out, int cuda_device);
+/* Replaces GraphicsDevice::Destruct for the tracer's resources. */
+void tracer_destroy(tracer_ctx* ctx);
+const char* tracer_last_error(const tracer_ctx* ctx);
+const char* tracer_status_string(int status);
+/* Bound for every wait on the GPU (default 60000 ms). */
+int tracer_set_timeout(tracer_ctx* ctx, uint32_t timeout_ms);
+
+/* Replaces the scene SSBO upload (GraphicsDevice.cpp:796-822).  Copies the
+ * arrays to the GPU, building or validating BVHs; replaces any previous scene. */
+int tracer_upload_scene(tracer_ctx* ctx, const tracer_scene_desc* desc);
+
+/* Replaces the material table of the current scene in place (same count). */
+int tracer_set_materials(tracer_ctx* ctx, const tracer_material* materials, uint32_t num_materials);
+
+/* Replaces vkCmdPushConstants + vkCmdDispatch (GraphicsDevice.cpp:1264-1266).
+ * Asynchronous and ordered on cuda_stream (a cudaStream_t; NULL = the
+ * context's own stream).  frame is copied by value, like a push constant. */
+int tracer_trace(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params, void* cuda_stream);
+
+/* Waits (bounded) for the last trace, reports device-side errors, and copies
+ * one AOV to host memory; bytes must equal the AOV's size. */
+int tracer_readback(tracer_ctx* ctx, int aov, void* host_dst, size_t bytes);
+
+/* Waits (bounded) for the last trace and reports device-side errors. */
+int tracer_synchronize(tracer_ctx* ctx);
+
+/* Device address and size of an AOV of the last trace (zero-copy interop;
+ * valid until the next trace with a different image size). */
+int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRACER_ABI_H */

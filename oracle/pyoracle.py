@@ -1,0 +1,231 @@
+"""Python wrapper of the CPU oracle and of the reference-shader harness.
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, to check or time the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+STATS_FIELDS = ["closest_rays", "shadow_rays", "node_fetches", "tri_tests", "sphere_tests", "plane_tests", "hits"]
+
+
+class OScene(ctypes.Structure):
+    _fields_ = [("triangles", ctypes.c_void_p), ("num_triangles", ctypes.c_uint32),
+                ("materials", ctypes.c_void_p), ("num_materials", ctypes.c_uint32),
+                ("spheres", ctypes.c_void_p), ("num_spheres", ctypes.c_uint32),
+                ("planes", ctypes.c_void_p), ("num_planes", ctypes.c_uint32),
+                ("tri_nodes", ctypes.c_void_p), ("num_tri_nodes", ctypes.c_uint32),
+                ("tri_prim_index", ctypes.c_void_p),
+                ("sphere_nodes", ctypes.c_void_p), ("num_sphere_nodes", ctypes.c_uint32),
+                ("sphere_prim_index", ctypes.c_void_p)]
+
+
+class OParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32),
+                ("max_depth", ctypes.c_uint32), ("rr_start", ctypes.c_uint32), ("sky", ctypes.c_float * 3),
+                ("tie_mode", ctypes.c_int32), ("trig_mode", ctypes.c_int32), ("threads", ctypes.c_int32),
+                ("row_begin", ctypes.c_uint32), ("row_end", ctypes.c_uint32), ("row_step", ctypes.c_uint32)]
+
+
+class OStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in STATS_FIELDS]
+
+
+def build() -> str:
+    """Builds liboracle.so (make -C oracle)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def build_ref() -> bool:
+    """Builds the reference-shader harness when the reference tree exists."""
+    if not os.path.isdir("/root/reference/Assets"):
+        return False
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"OUT={REF_DIR}"], check=True)
+    return True
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        vp, f32, i32 = ctypes.c_void_p, ctypes.c_float, ctypes.c_int
+        L.oracle_render.argtypes = [ctypes.POINTER(OScene), vp, ctypes.POINTER(OParams), vp, vp, vp, vp,
+                                    ctypes.POINTER(OStats)]
+        L.oracle_render_f64.argtypes = [ctypes.POINTER(OScene), vp, ctypes.POINTER(OParams), vp, vp,
+                                        ctypes.POINTER(OStats)]
+        L.oracle_rand.argtypes = [f32, f32, f32, i32, i32, vp]
+        L.oracle_rand.restype = None
+        L.oracle_cos.argtypes = [f32]
+        L.oracle_cos.restype = f32
+        L.oracle_sin.argtypes = [f32]
+        L.oracle_sin.restype = f32
+        for fn in ("oracle_tri_intersect",):
+            getattr(L, fn).argtypes = [vp, vp, vp]
+            getattr(L, fn).restype = f32
+        L.oracle_sphere_intersect.argtypes = [vp, vp, vp, f32]
+        L.oracle_sphere_intersect.restype = f32
+        L.oracle_plane_intersect.argtypes = [vp, vp, vp, f32]
+        L.oracle_plane_intersect.restype = f32
+        L.oracle_trace_ray.argtypes = [ctypes.POINTER(OScene), i32, i32, vp, vp, f32, vp, ctypes.POINTER(OStats)]
+        L.oracle_radiance.argtypes = [ctypes.POINTER(OScene), vp, ctypes.POINTER(OParams), vp, vp, f32, f32, f32,
+                                      vp, vp]
+        L.oracle_radiance.restype = None
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None or a.size == 0 else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _SceneRef:
+    """Keeps numpy arrays alive while the oracle reads them."""
+
+    def __init__(self, sc, tri_bvh=None, sphere_bvh=None):
+        self.arrs = [np.ascontiguousarray(a) for a in (sc.triangles, sc.materials, sc.spheres, sc.planes)]
+        self.s = OScene()
+        s = self.s
+        s.triangles, s.num_triangles = _p(self.arrs[0]), len(self.arrs[0])
+        s.materials, s.num_materials = _p(self.arrs[1]), len(self.arrs[1])
+        s.spheres, s.num_spheres = _p(self.arrs[2]), len(self.arrs[2])
+        s.planes, s.num_planes = _p(self.arrs[3]), len(self.arrs[3])
+        if tri_bvh is not None:
+            n, i = np.ascontiguousarray(tri_bvh[0]), np.ascontiguousarray(tri_bvh[1], np.uint32)
+            self.arrs += [n, i]
+            s.tri_nodes, s.num_tri_nodes, s.tri_prim_index = _p(n), len(n), _p(i)
+        if sphere_bvh is not None:
+            n, i = np.ascontiguousarray(sphere_bvh[0]), np.ascontiguousarray(sphere_bvh[1], np.uint32)
+            self.arrs += [n, i]
+            s.sphere_nodes, s.num_sphere_nodes, s.sphere_prim_index = _p(n), len(n), _p(i)
+
+
+def params(width, height, spp=4, max_depth=4, rr_start=0, sky=(0.0, 0.0, 0.0), tie_mode=1, trig_mode=0, threads=0,
+           rows=None) -> OParams:
+    p = OParams()
+    p.width, p.height, p.spp, p.max_depth, p.rr_start = width, height, spp, max_depth, rr_start
+    p.sky = (ctypes.c_float * 3)(*sky)
+    p.tie_mode, p.trig_mode, p.threads = tie_mode, trig_mode, threads
+    if rows is not None:
+        p.row_begin, p.row_end, p.row_step = rows
+    return p
+
+
+def render(sc, frame, prm: OParams, tri_bvh=None, sphere_bvh=None):
+    """Renders with the oracle; returns dict(rgba32f, rgba8, hit_id, hit_t, stats)."""
+    L = lib()
+    ref = _SceneRef(sc, tri_bvh, sphere_bvh)
+    f = np.ascontiguousarray(frame).reshape(())
+    h, w = prm.height, prm.width
+    rgba = np.zeros((h, w, 4), np.float32)
+    u8 = np.zeros((h, w, 4), np.uint8)
+    hid = np.full((h, w), 0xFFFFFFFF, np.uint32)
+    ht = np.full((h, w), -1.0, np.float32)
+    st = OStats()
+    L.oracle_render(ctypes.byref(ref.s), f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(prm), _p(rgba), _p(u8),
+                    _p(hid), _p(ht), ctypes.byref(st))
+    return {"rgba32f": rgba, "rgba8": u8, "hit_id": hid, "hit_t": ht,
+            "stats": {k: int(getattr(st, k)) for k in STATS_FIELDS}}
+
+
+def rand(cx, cy, salt, n, trig_mode=0):
+    out = np.zeros(n, np.float32)
+    lib().oracle_rand(cx, cy, salt, trig_mode, n, _p(out))
+    return out
+
+
+def trace_ray(sc, o, d, tmax, tie_mode=1, shadow=False, tri_bvh=None, sphere_bvh=None):
+    L = lib()
+    ref = _SceneRef(sc, tri_bvh, sphere_bvh)
+    o = np.asarray(o, np.float32)
+    d = np.asarray(d, np.float32)
+    out = np.zeros(21, np.float32)
+    st = OStats()
+    found = L.oracle_trace_ray(ctypes.byref(ref.s), tie_mode, int(shadow), _p(o), _p(d), tmax, _p(out),
+                               ctypes.byref(st))
+    return {"found": bool(found), "t": float(out[1]), "P": out[2:5].copy(), "N": out[5:8].copy(),
+            "material": out[8:20].copy(), "prim": int(out[20:21].view(np.uint32)[0]),
+            "stats": {k: int(getattr(st, k)) for k in STATS_FIELDS}}
+
+
+# ------------------------------------------------------- reference harness --
+class RefHarness:
+    """The reference shader compiled for the host (oracle/ref/Makefile)."""
+
+    def __init__(self, rng_trig: bool = False):
+        name = "libref_tracer_rngtrig.so" if rng_trig else "libref_tracer.so"
+        path = os.path.join(REF_DIR, name)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = ctypes.CDLL(path)
+        vp, f32, u32, i32 = ctypes.c_void_p, ctypes.c_float, ctypes.c_uint, ctypes.c_int
+        L.ref_render.argtypes = [vp, vp, u32, i32, i32, vp, vp]
+        L.ref_render.restype = None
+        L.ref_radiance.argtypes = [vp, vp, u32, vp, vp, f32, f32, f32, vp, vp]
+        L.ref_radiance.restype = None
+        L.ref_rand.argtypes = [f32, f32, f32, i32, vp]
+        L.ref_rand.restype = None
+        L.ref_trace_ray.argtypes = [vp, u32, vp, vp, f32, vp]
+        L.ref_trace_ray.restype = None
+        L.ref_tri_intersect.argtypes = [vp, vp, vp]
+        L.ref_tri_intersect.restype = f32
+        L.ref_sphere_intersect.argtypes = [vp, vp, vp, f32]
+        L.ref_sphere_intersect.restype = f32
+        L.ref_plane_intersect.argtypes = [vp, vp, vp, f32]
+        L.ref_plane_intersect.restype = f32
+        L.ref_scene_constants.argtypes = [vp, vp, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+        L.ref_scene_constants.restype = u32
+        self.L = L
+
+    def render(self, frame, triangles, w, h):
+        f = np.ascontiguousarray(frame).reshape(())
+        t = np.ascontiguousarray(triangles)
+        rgba = np.zeros((h, w, 4), np.float32)
+        u8 = np.zeros((h, w, 4), np.uint8)
+        self.L.ref_render(f.ctypes.data_as(ctypes.c_void_p), _p(t), len(t), w, h, _p(rgba), _p(u8))
+        return rgba, u8
+
+    def rand(self, cx, cy, salt, n):
+        out = np.zeros(n, np.float32)
+        self.L.ref_rand(cx, cy, salt, n, _p(out))
+        return out
+
+    def trace_ray(self, triangles, o, d, tmax):
+        t = np.ascontiguousarray(triangles)
+        out = np.zeros(20, np.float32)
+        self.L.ref_trace_ray(_p(t), len(t), _p(np.asarray(o, np.float32)), _p(np.asarray(d, np.float32)), tmax,
+                             _p(out))
+        return out
+
+    def scene_constants(self):
+        sph = np.zeros(16 * 16, np.float32)
+        pl = np.zeros(16 * 16, np.float32)
+        tm = np.zeros(12, np.float32)
+        ns, npl = ctypes.c_uint(), ctypes.c_uint()
+        code = self.L.ref_scene_constants(_p(sph), _p(pl), _p(tm), ctypes.byref(ns), ctypes.byref(npl))
+        return (sph[: 16 * ns.value].reshape(ns.value, 16), pl[: 16 * npl.value].reshape(npl.value, 16), tm,
+                divmod(code, 1000))
+
+
+def ref_camera(pos, pitch, yaw):
+    L = ctypes.CDLL(os.path.join(REF_DIR, "libref_camera.so"))
+    out = np.zeros(16, np.float32)
+    f32 = ctypes.c_float
+    L.ref_camera.argtypes = [f32, f32, f32, f32, f32, ctypes.c_void_p]
+    L.ref_camera.restype = None
+    L.ref_camera(pos[0], pos[1], pos[2], pitch, yaw, _p(out))
+    return out

@@ -558,7 +558,7 @@ template <class T> struct Tracer {
             }
         }
         if (h.kind == 0) return false;
-        st.hits++;
+        if (!shadow) st.hits++;  // closest-hit rays that hit (each reads a material record)
         is.t = h.t;
         is.prim = h.prim;
         is.P = ray.origin + h.t * ray.dir;

@@ -1,0 +1,498 @@
+// Host side of the C ABI (include/tracer_abi.h): context, scene upload,
+// trace launch, bounded waits and readback.
+//
+// Replaces the compute portion of GraphicsDevice (Source/GraphicsDevice.cpp):
+// scene SSBO creation and upload (:796-822), compute pipeline with the
+// 96-byte push-constant range (:1089-1131), and the per-frame bind, push and
+// dispatch (:1254-1266).  Where the reference ignores most Vulkan results and
+// waits on fences forever (:1217), every call here returns a status and every
+// wait on the GPU is bounded.
+
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "tracer_abi.h"
+#include "tracer_core.cuh"
+#include "tracer_launch.h"
+
+using namespace vkt;
+
+namespace {
+
+template <class T> struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct SceneBuffers {
+    DevBuf<float4> tri, mats, sph_geo, sph_rec, planes, tri_nodes, sph_nodes;
+    DevBuf<uint32_t> sph_id, emit;
+    uint32_t nt = 0, nm = 0, ns = 0, np = 0, ne = 0;
+    uint32_t n_tri_nodes = 0, n_sph_nodes = 0;
+    uint32_t depth = 0;  // deepest BVH
+    bool bvh = false;
+    bool loaded = false;
+    void release()
+    {
+        tri.release();
+        mats.release();
+        sph_geo.release();
+        sph_rec.release();
+        planes.release();
+        tri_nodes.release();
+        sph_nodes.release();
+        sph_id.release();
+        emit.release();
+        *this = SceneBuffers();
+    }
+};
+
+}  // namespace
+
+struct tracer_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    uint32_t timeout_ms = 60000;
+    std::string err;
+    SceneBuffers scene;
+    // frame outputs
+    uint32_t width = 0, height = 0;
+    DevBuf<uchar4> rgba8;
+    DevBuf<float4> rgba32f;
+    DevBuf<uint2> hit;
+    DevBuf<unsigned long long> stats;
+    DevBuf<int> status;
+    DevBuf<uint32_t> work;
+    uint32_t last_mask = 0;
+};
+
+namespace {
+
+int fail(tracer_ctx* c, int code, const char* fmt, ...)
+{
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(tracer_ctx* c, cudaError_t e, const char* what)
+{
+    if (e == cudaErrorMemoryAllocation) return fail(c, TRACER_ERR_OOM, "%s: out of device memory", what);
+    return fail(c, TRACER_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+template <class T> cudaError_t dalloc(DevBuf<T>& b, size_t n)
+{
+    if (b.n == n && b.p) return cudaSuccess;
+    b.release();
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&b.p, n * sizeof(T));
+    if (e == cudaSuccess) b.n = n;
+    return e;
+}
+
+template <class T> cudaError_t upload(DevBuf<T>& b, const T* src, size_t n)
+{
+    cudaError_t e = dalloc(b, n);
+    if (e != cudaSuccess || n == 0) return e;
+    return cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// Bounded wait on an event: polls instead of blocking so a stuck GPU turns
+// into TRACER_ERR_TIMEOUT rather than a hang.
+int wait_event(tracer_ctx* c, cudaEvent_t ev)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess) return TRACER_OK;
+        if (e != cudaErrorNotReady) return cuda_fail(c, e, "waiting for the GPU");
+        auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+        if (ms > (long long)c->timeout_ms)
+            return fail(c, TRACER_ERR_TIMEOUT, "GPU did not finish within %u ms", c->timeout_ms);
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int finish(tracer_ctx* c)
+{
+    if (!c->pending) return TRACER_OK;
+    int r = wait_event(c, c->done);
+    if (r != TRACER_OK) return r;
+    c->pending = false;
+    int st = 0;
+    cudaError_t e = cudaMemcpy(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "reading the device status");
+    if (st == ST_TRAVERSAL_LIMIT)
+        return fail(c, TRACER_ERR_TRAVERSAL_LIMIT, "a ray exceeded the BVH traversal step limit");
+    if (st == ST_STACK_OVERFLOW)
+        return fail(c, TRACER_ERR_STACK_OVERFLOW, "traversal stack depth too small for the BVH");
+    return TRACER_OK;
+}
+
+// Builds (or validates) one BVH; returns the leaf-order permutation.
+int prepare_bvh(tracer_ctx* c, int kind, int prim_type, const void* prims, uint32_t n, uint32_t leaf, uint32_t bins,
+                const tracer_bvh_node* given, uint32_t n_given, const uint32_t* given_idx,
+                std::vector<tracer_bvh_node>& nodes, std::vector<uint32_t>& idx, uint32_t& depth)
+{
+    if (given) {
+        if (!given_idx) return fail(c, TRACER_ERR_INVALID_ARG, "prebuilt BVH without a primitive index array");
+        int r = tracer_validate_bvh(prim_type, prims, n, given, n_given, given_idx, &depth);
+        if (r != TRACER_OK) return fail(c, TRACER_ERR_BAD_BVH, "prebuilt BVH failed validation");
+        nodes.assign(given, given + n_given);
+        idx.assign(given_idx, given_idx + n);
+        return TRACER_OK;
+    }
+    nodes.resize(2 * (size_t)n);
+    idx.resize(n);
+    uint32_t nn = 0;
+    int r = tracer_build_bvh(kind, prim_type, prims, n, leaf, bins, nodes.data(), &nn, idx.data(), &depth);
+    if (r != TRACER_OK) return fail(c, r, "BVH build failed");
+    nodes.resize(nn);
+    return TRACER_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tracer_status_string(int s)
+{
+    switch (s) {
+    case TRACER_OK: return "ok";
+    case TRACER_ERR_NO_SUITABLE_GPU: return "no suitable GPU";
+    case TRACER_ERR_NO_SUITABLE_SURFACE: return "no suitable surface";
+    case TRACER_ERR_UNKNOWN: return "unknown error";
+    case TRACER_ERR_INVALID_ARG: return "invalid argument";
+    case TRACER_ERR_OOM: return "out of memory";
+    case TRACER_ERR_TIMEOUT: return "timeout";
+    case TRACER_ERR_TRAVERSAL_LIMIT: return "traversal step limit exceeded";
+    case TRACER_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+    case TRACER_ERR_CUDA: return "CUDA error";
+    case TRACER_ERR_NO_SCENE: return "no scene uploaded";
+    case TRACER_ERR_BAD_BVH: return "invalid BVH";
+    default: return "unrecognised status";
+    }
+}
+
+int tracer_create(tracer_ctx** out, int cuda_device)
+{
+    if (!out) return TRACER_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return TRACER_ERR_NO_SUITABLE_GPU;
+    if (cuda_device < 0 || cuda_device >= n) return TRACER_ERR_NO_SUITABLE_GPU;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, cuda_device) != cudaSuccess) return TRACER_ERR_NO_SUITABLE_GPU;
+    // The kernels are built for sm_103a only.
+    if (prop.major != 10) return TRACER_ERR_NO_SUITABLE_GPU;
+    if (cudaSetDevice(cuda_device) != cudaSuccess) return TRACER_ERR_NO_SUITABLE_GPU;
+    tracer_ctx* c = new tracer_ctx();
+    c->device = cuda_device;
+    c->sm_count = prop.multiProcessorCount;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = dalloc(c->stats, C_COUNT);
+    if (e == cudaSuccess) e = dalloc(c->status, 1);
+    if (e == cudaSuccess) e = dalloc(c->work, 1);
+    if (e != cudaSuccess) {
+        tracer_destroy(c);
+        return e == cudaErrorMemoryAllocation ? TRACER_ERR_OOM : TRACER_ERR_CUDA;
+    }
+    *out = c;
+    return TRACER_OK;
+}
+
+void tracer_destroy(tracer_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->pending && c->done) wait_event(c, c->done);
+    c->scene.release();
+    c->rgba8.release();
+    c->rgba32f.release();
+    c->hit.release();
+    c->stats.release();
+    c->status.release();
+    c->work.release();
+    if (c->done) cudaEventDestroy(c->done);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* tracer_last_error(const tracer_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int tracer_set_timeout(tracer_ctx* c, uint32_t ms)
+{
+    if (!c || ms == 0) return TRACER_ERR_INVALID_ARG;
+    c->timeout_ms = ms;
+    return TRACER_OK;
+}
+
+int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!d) return fail(c, TRACER_ERR_INVALID_ARG, "null scene description");
+    if (d->num_triangles && !d->triangles) return fail(c, TRACER_ERR_INVALID_ARG, "null triangle array");
+    if (d->num_spheres && !d->spheres) return fail(c, TRACER_ERR_INVALID_ARG, "null sphere array");
+    if (d->num_planes && !d->planes) return fail(c, TRACER_ERR_INVALID_ARG, "null plane array");
+    if (d->num_materials && !d->materials) return fail(c, TRACER_ERR_INVALID_ARG, "null material array");
+    if (d->bvh != TRACER_BVH_NONE && d->bvh != TRACER_BVH_MEDIAN && d->bvh != TRACER_BVH_SAH)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown BVH kind %d", d->bvh);
+    if ((uint64_t)d->num_triangles + d->num_spheres + d->num_planes >= 0xFFFFFFFFull)
+        return fail(c, TRACER_ERR_INVALID_ARG, "too many primitives");
+    for (uint32_t i = 0; i < d->num_triangles; ++i)
+        if (d->triangles[i].material >= d->num_materials)
+            return fail(c, TRACER_ERR_INVALID_ARG, "triangle %u uses material %u of %u", i, d->triangles[i].material,
+                        d->num_materials);
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    SceneBuffers& s = c->scene;
+    s.release();
+    s.nt = d->num_triangles;
+    s.nm = d->num_materials;
+    s.ns = d->num_spheres;
+    s.np = d->num_planes;
+    s.bvh = d->bvh != TRACER_BVH_NONE;
+
+    // Triangles in traversal order: (v0, material) (v1 - v0, id) (v2 - v0, 0)
+    std::vector<tracer_bvh_node> tnodes, snodes;
+    std::vector<uint32_t> tidx, sidx;
+    uint32_t tdepth = 0, sdepth = 0;
+    if (s.bvh && s.nt) {
+        r = prepare_bvh(c, d->bvh, TRACER_PRIM_TRIANGLE, d->triangles, s.nt, d->leaf_size, d->sah_bins, d->tri_nodes,
+                        d->num_tri_nodes, d->tri_prim_index, tnodes, tidx, tdepth);
+        if (r != TRACER_OK) return r;
+    }
+    if (s.bvh && s.ns) {
+        r = prepare_bvh(c, d->bvh, TRACER_PRIM_SPHERE, d->spheres, s.ns, d->leaf_size, d->sah_bins, d->sphere_nodes,
+                        d->num_sphere_nodes, d->sphere_prim_index, snodes, sidx, sdepth);
+        if (r != TRACER_OK) return r;
+    }
+    std::vector<float4> tri(3 * (size_t)s.nt);
+    for (uint32_t k = 0; k < s.nt; ++k) {
+        const uint32_t i = s.bvh ? tidx[k] : k;
+        const tracer_triangle& t = d->triangles[i];
+        float m, id;
+        std::memcpy(&m, &t.material, 4);
+        std::memcpy(&id, &i, 4);
+        tri[3 * k + 0] = make_float4(t.v0[0], t.v0[1], t.v0[2], m);
+        tri[3 * k + 1] = make_float4(t.v1[0] - t.v0[0], t.v1[1] - t.v0[1], t.v1[2] - t.v0[2], id);
+        tri[3 * k + 2] = make_float4(t.v2[0] - t.v0[0], t.v2[1] - t.v0[1], t.v2[2] - t.v0[2], 0.0f);
+    }
+    std::vector<float4> geo(s.ns);
+    std::vector<uint32_t> sid(s.ns), emit;
+    for (uint32_t k = 0; k < s.ns; ++k) {
+        const uint32_t i = s.bvh ? sidx[k] : k;
+        const tracer_sphere& q = d->spheres[i];
+        geo[k] = make_float4(q.P[0], q.P[1], q.P[2], q.r);
+        sid[k] = i;
+    }
+    for (uint32_t i = 0; i < s.ns; ++i) {
+        const float* em = d->spheres[i].mat.emissive;
+        if (!(em[0] == 0.0f && em[1] == 0.0f && em[2] == 0.0f)) emit.push_back(i);
+    }
+    s.ne = (uint32_t)emit.size();
+    s.n_tri_nodes = (uint32_t)tnodes.size();
+    s.n_sph_nodes = (uint32_t)snodes.size();
+    s.depth = tdepth > sdepth ? tdepth : sdepth;
+
+    cudaError_t e = upload(s.tri, tri.data(), tri.size());
+    if (e == cudaSuccess) e = upload(s.mats, reinterpret_cast<const float4*>(d->materials), 3 * (size_t)s.nm);
+    if (e == cudaSuccess) e = upload(s.sph_geo, geo.data(), geo.size());
+    if (e == cudaSuccess) e = upload(s.sph_id, sid.data(), sid.size());
+    if (e == cudaSuccess) e = upload(s.sph_rec, reinterpret_cast<const float4*>(d->spheres), 4 * (size_t)s.ns);
+    if (e == cudaSuccess) e = upload(s.planes, reinterpret_cast<const float4*>(d->planes), 4 * (size_t)s.np);
+    if (e == cudaSuccess) e = upload(s.emit, emit.data(), emit.size());
+    if (e == cudaSuccess)
+        e = upload(s.tri_nodes, reinterpret_cast<const float4*>(tnodes.data()), 2 * tnodes.size());
+    if (e == cudaSuccess)
+        e = upload(s.sph_nodes, reinterpret_cast<const float4*>(snodes.data()), 2 * snodes.size());
+    if (e != cudaSuccess) {
+        s.release();
+        return cuda_fail(c, e, "scene upload");
+    }
+    s.loaded = true;
+    return TRACER_OK;
+}
+
+int tracer_set_materials(tracer_ctx* c, const tracer_material* mats, uint32_t n)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!c->scene.loaded) return fail(c, TRACER_ERR_NO_SCENE, "no scene uploaded");
+    if (!mats || n != c->scene.nm) return fail(c, TRACER_ERR_INVALID_ARG, "material count %u != %u", n, c->scene.nm);
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaError_t e = cudaMemcpy(c->scene.mats.p, mats, sizeof(tracer_material) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "material update");
+    return TRACER_OK;
+}
+
+int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params* p, void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!f || !p) return fail(c, TRACER_ERR_INVALID_ARG, "null frame or params");
+    if (!c->scene.loaded) return fail(c, TRACER_ERR_NO_SCENE, "no scene uploaded");
+    if (p->width == 0 || p->height == 0 || p->width > 32768 || p->height > 32768)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "image size %ux%u not supported", p->width, p->height);
+    if (p->spp == 0 || p->max_depth == 0 || p->max_depth > 1024 || p->spp > 1u << 20)
+        return fail(c, TRACER_ERR_INVALID_ARG, "spp %u / max_depth %u out of range", p->spp, p->max_depth);
+    if (p->tie_mode != TRACER_TIES_REFERENCE && p->tie_mode != TRACER_TIES_STRICT)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
+    if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
+        return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
+    int kernel = p->kernel == TRACER_KERNEL_AUTO ? TRACER_KERNEL_PERSISTENT : p->kernel;
+    if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_PERSISTENT)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
+    uint32_t block = p->block ? p->block : 128;
+    if (block % 32 != 0 || block < 32 || block > 256)
+        return fail(c, TRACER_ERR_INVALID_ARG, "block %u must be a multiple of 32 in [32, 256]", block);
+    uint32_t need = c->scene.bvh ? (c->scene.depth > 1 ? c->scene.depth : 1) : 0;
+    uint32_t stack = p->stack_depth ? p->stack_depth : need;
+    if (c->scene.bvh && stack < need)
+        return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
+    if ((size_t)stack * block * 8 > 200 * 1024)
+        return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u x block %u exceeds shared memory", stack, block);
+    const uint32_t mask = p->aov_mask ? p->aov_mask : (1u << TRACER_AOV_RGBA8);
+    if (mask & ~((1u << TRACER_AOV_RGBA8) | (1u << TRACER_AOV_RGBA32F) | (1u << TRACER_AOV_PRIMARY_HIT) |
+                 (1u << TRACER_AOV_STATS)))
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "unknown AOV in mask 0x%x", mask);
+
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    const size_t npx = (size_t)p->width * p->height;
+    cudaError_t e = cudaSuccess;
+    if (mask & (1u << TRACER_AOV_RGBA8)) e = dalloc(c->rgba8, npx);
+    if (e == cudaSuccess && (mask & (1u << TRACER_AOV_RGBA32F))) e = dalloc(c->rgba32f, npx);
+    if (e == cudaSuccess && (mask & (1u << TRACER_AOV_PRIMARY_HIT))) e = dalloc(c->hit, npx);
+    if (e != cudaSuccess) return cuda_fail(c, e, "image allocation");
+    c->width = p->width;
+    c->height = p->height;
+    c->last_mask = mask;
+
+    TraceArgs a;
+    std::memset(&a, 0, sizeof a);
+    const SceneBuffers& s = c->scene;
+    a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
+                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes};
+    a.fr.aspect = f->aspect_ratio;
+    a.fr.seed = f->seed;
+    const tracer_camera& cam = f->camera;
+    a.fr.cpos = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
+    a.fr.cdir = V3{cam.dir[0], cam.dir[1], cam.dir[2]};
+    a.fr.cright = V3{cam.right[0], cam.right[1], cam.right[2]};
+    a.fr.cup = V3{cam.up[0], cam.up[1], cam.up[2]};
+    a.width = p->width;
+    a.height = p->height;
+    a.spp = p->spp;
+    a.max_depth = p->max_depth;
+    a.rr_start = p->rr_start;
+    a.sky = V3{p->sky[0], p->sky[1], p->sky[2]};
+    a.sky_on = !(p->sky[0] == 0.0f && p->sky[1] == 0.0f && p->sky[2] == 0.0f);
+    a.stack_depth = stack;
+    const uint32_t nn = s.n_tri_nodes > s.n_sph_nodes ? s.n_tri_nodes : s.n_sph_nodes;
+    a.trav_limit = 2 * nn + 16;
+    a.rgba8 = (mask & (1u << TRACER_AOV_RGBA8)) ? c->rgba8.p : nullptr;
+    a.rgba32f = (mask & (1u << TRACER_AOV_RGBA32F)) ? c->rgba32f.p : nullptr;
+    a.hit = (mask & (1u << TRACER_AOV_PRIMARY_HIT)) ? c->hit.p : nullptr;
+    a.stats = c->stats.p;
+    a.status = c->status.p;
+    a.work = c->work.p;
+    a.num_pixels = persistent_ids(p->width, p->height);
+
+    LaunchConfig lc;
+    lc.kernel = kernel;
+    lc.block = block;
+    lc.stats = (p->stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
+    lc.tie = p->tie_mode;
+    lc.bvh = s.bvh ? 1 : 0;
+    lc.grid = 0;
+    if (kernel == TRACER_KERNEL_PERSISTENT) {
+        int per = persistent_blocks_per_sm(lc, stack, lc.stats, lc.bvh, lc.tie);
+        if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "persistent kernel cannot be resident with block %u", block);
+        if (p->wavefront && (int)p->wavefront < per) per = (int)p->wavefront;
+        lc.grid = (uint32_t)(per * c->sm_count);
+    }
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->work.p, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = launch_trace(a, lc, st);
+    if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "trace launch");
+    c->pending = true;
+    return TRACER_OK;
+}
+
+int tracer_synchronize(tracer_ctx* c)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    return finish(c);
+}
+
+static int aov_info(tracer_ctx* c, int aov, void** ptr, size_t* bytes)
+{
+    const size_t npx = (size_t)c->width * c->height;
+    const uint32_t bit = aov >= 0 && aov < 32 ? (1u << aov) : 0;
+    if (!bit || !(c->last_mask & bit) || c->width == 0)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "AOV %d was not produced by the last trace", aov);
+    switch (aov) {
+    case TRACER_AOV_RGBA8: *ptr = c->rgba8.p; *bytes = npx * 4; break;
+    case TRACER_AOV_RGBA32F: *ptr = c->rgba32f.p; *bytes = npx * 16; break;
+    case TRACER_AOV_PRIMARY_HIT: *ptr = c->hit.p; *bytes = npx * 8; break;
+    case TRACER_AOV_STATS: *ptr = c->stats.p; *bytes = sizeof(tracer_stats); break;
+    default: return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "unknown AOV %d", aov);
+    }
+    return TRACER_OK;
+}
+
+int tracer_readback(tracer_ctx* c, int aov, void* dst, size_t bytes)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!dst) return fail(c, TRACER_ERR_INVALID_ARG, "null destination");
+    cudaSetDevice(c->device);
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    void* src;
+    size_t n;
+    r = aov_info(c, aov, &src, &n);
+    if (r != TRACER_OK) return r;
+    if (bytes != n) return fail(c, TRACER_ERR_INVALID_ARG, "AOV %d holds %zu bytes, %zu requested", aov, n, bytes);
+    cudaError_t e = cudaMemcpy(dst, src, n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "readback");
+    return TRACER_OK;
+}
+
+int tracer_device_image(tracer_ctx* c, int aov, void** ptr, size_t* bytes)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!ptr || !bytes) return fail(c, TRACER_ERR_INVALID_ARG, "null output");
+    return aov_info(c, aov, ptr, bytes);
+}
+
+}  // extern "C"

@@ -1,0 +1,242 @@
+"""ctypes binding of the C ABI (include/tracer_abi.h) and a thin Python
+mirror of the reference's per-frame interface.
+
+The library must exist (``vktrace._build.build()`` makes it); there is no
+fallback: a missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import scene as S
+from ._build import LIB_PATH
+
+OK = 0
+ERR_NO_SUITABLE_GPU = -1
+ERR_NO_SUITABLE_SURFACE = -2
+ERR_UNKNOWN = -3
+ERR_INVALID_ARG = -4
+ERR_OOM = -5
+ERR_TIMEOUT = -6
+ERR_TRAVERSAL_LIMIT = -7
+ERR_STACK_OVERFLOW = -8
+ERR_CUDA = -9
+ERR_NO_SCENE = -10
+ERR_BAD_BVH = -11
+
+TIES_REFERENCE, TIES_STRICT = 0, 1
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_PERSISTENT = 0, 1, 2
+AOV_RGBA8, AOV_RGBA32F, AOV_PRIMARY_HIT, AOV_STATS = 0, 1, 2, 3
+PRIM_TRIANGLE, PRIM_SPHERE = 0, 1
+
+STATS_FIELDS = ["closest_rays", "shadow_rays", "node_fetches", "tri_tests", "sphere_tests", "plane_tests", "hits"]
+
+EXPORTED_SYMBOLS = [
+    "tracer_create", "tracer_destroy", "tracer_last_error", "tracer_status_string", "tracer_set_timeout",
+    "tracer_upload_scene", "tracer_set_materials", "tracer_trace", "tracer_readback", "tracer_synchronize",
+    "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh",
+]
+
+
+class TracerError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [
+        ("triangles", ctypes.c_void_p), ("num_triangles", ctypes.c_uint32),
+        ("materials", ctypes.c_void_p), ("num_materials", ctypes.c_uint32),
+        ("spheres", ctypes.c_void_p), ("num_spheres", ctypes.c_uint32),
+        ("planes", ctypes.c_void_p), ("num_planes", ctypes.c_uint32),
+        ("bvh", ctypes.c_int32), ("leaf_size", ctypes.c_uint32), ("sah_bins", ctypes.c_uint32),
+        ("tri_nodes", ctypes.c_void_p), ("num_tri_nodes", ctypes.c_uint32), ("tri_prim_index", ctypes.c_void_p),
+        ("sphere_nodes", ctypes.c_void_p), ("num_sphere_nodes", ctypes.c_uint32),
+        ("sphere_prim_index", ctypes.c_void_p),
+    ]
+
+
+class TraceParams(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32),
+        ("max_depth", ctypes.c_uint32), ("rr_start", ctypes.c_uint32), ("sky", ctypes.c_float * 3),
+        ("tie_mode", ctypes.c_int32), ("kernel", ctypes.c_int32), ("block", ctypes.c_uint32),
+        ("stack_depth", ctypes.c_uint32), ("wavefront", ctypes.c_uint32), ("aov_mask", ctypes.c_uint32),
+        ("stats", ctypes.c_uint32),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Loads libtracer.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"CUDA library not built: {p} (run vktrace._build.build())")
+    lib = ctypes.CDLL(p)
+    vp, u32, i32, sz = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_size_t
+    lib.tracer_create.argtypes = [ctypes.POINTER(vp), i32]
+    lib.tracer_destroy.argtypes = [vp]
+    lib.tracer_destroy.restype = None
+    lib.tracer_last_error.argtypes = [vp]
+    lib.tracer_last_error.restype = ctypes.c_char_p
+    lib.tracer_status_string.argtypes = [i32]
+    lib.tracer_status_string.restype = ctypes.c_char_p
+    lib.tracer_set_timeout.argtypes = [vp, u32]
+    lib.tracer_upload_scene.argtypes = [vp, ctypes.POINTER(SceneDesc)]
+    lib.tracer_set_materials.argtypes = [vp, vp, u32]
+    lib.tracer_trace.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp]
+    lib.tracer_readback.argtypes = [vp, i32, vp, sz]
+    lib.tracer_synchronize.argtypes = [vp]
+    lib.tracer_device_image.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(sz)]
+    lib.tracer_build_bvh.argtypes = [i32, i32, vp, u32, u32, u32, vp, ctypes.POINTER(u32), vp, ctypes.POINTER(u32)]
+    lib.tracer_validate_bvh.argtypes = [i32, vp, u32, vp, u32, vp, ctypes.POINTER(u32)]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None or a.size == 0 else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def build_bvh(kind: int, prims: np.ndarray, leaf_size: int = 0, sah_bins: int = 0):
+    """Runs the library's host BVH builder; returns (nodes, prim_index, depth)."""
+    lib = load_library()
+    prims = np.ascontiguousarray(prims)
+    ptype = PRIM_TRIANGLE if prims.dtype == S.TRIANGLE else PRIM_SPHERE
+    n = len(prims)
+    nodes = np.zeros(max(1, 2 * n), S.BVH_NODE)
+    idx = np.zeros(n, np.uint32)
+    nn, depth = ctypes.c_uint32(), ctypes.c_uint32()
+    r = lib.tracer_build_bvh(kind, ptype, _ptr(prims), n, leaf_size, sah_bins, _ptr(nodes), ctypes.byref(nn),
+                             _ptr(idx), ctypes.byref(depth))
+    if r != OK:
+        raise TracerError(r, lib.tracer_status_string(r).decode())
+    return nodes[: nn.value].copy(), idx, depth.value
+
+
+def validate_bvh(prims: np.ndarray, nodes: np.ndarray, idx: np.ndarray) -> int:
+    lib = load_library()
+    ptype = PRIM_TRIANGLE if prims.dtype == S.TRIANGLE else PRIM_SPHERE
+    depth = ctypes.c_uint32()
+    r = lib.tracer_validate_bvh(ptype, _ptr(prims), len(prims), _ptr(nodes), len(nodes), _ptr(idx),
+                                ctypes.byref(depth))
+    if r != OK:
+        raise TracerError(r, lib.tracer_status_string(r).decode())
+    return depth.value
+
+
+class Tracer:
+    """One tracer context on one CUDA device (tracer_create .. tracer_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        r = self.lib.tracer_create(ctypes.byref(h), device)
+        if r != OK:
+            raise TracerError(r, self.lib.tracer_status_string(r).decode())
+        self.h = h
+        self.width = self.height = 0
+        self._scene_keep = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tracer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, r: int):
+        if r != OK:
+            raise TracerError(r, self.lib.tracer_last_error(self.h).decode())
+
+    def set_timeout(self, ms: int):
+        self._check(self.lib.tracer_set_timeout(self.h, ms))
+
+    def upload_scene(self, sc: S.Scene, tri_bvh=None, sphere_bvh=None):
+        arrs = [np.ascontiguousarray(a) for a in (sc.triangles, sc.materials, sc.spheres, sc.planes)]
+        d = SceneDesc()
+        d.triangles, d.num_triangles = _ptr(arrs[0]), len(arrs[0])
+        d.materials, d.num_materials = _ptr(arrs[1]), len(arrs[1])
+        d.spheres, d.num_spheres = _ptr(arrs[2]), len(arrs[2])
+        d.planes, d.num_planes = _ptr(arrs[3]), len(arrs[3])
+        d.bvh, d.leaf_size, d.sah_bins = sc.bvh, sc.leaf_size, sc.sah_bins
+        keep = list(arrs)
+        if tri_bvh is not None:
+            nodes, idx = np.ascontiguousarray(tri_bvh[0]), np.ascontiguousarray(tri_bvh[1], np.uint32)
+            d.tri_nodes, d.num_tri_nodes, d.tri_prim_index = _ptr(nodes), len(nodes), _ptr(idx)
+            keep += [nodes, idx]
+        if sphere_bvh is not None:
+            nodes, idx = np.ascontiguousarray(sphere_bvh[0]), np.ascontiguousarray(sphere_bvh[1], np.uint32)
+            d.sphere_nodes, d.num_sphere_nodes, d.sphere_prim_index = _ptr(nodes), len(nodes), _ptr(idx)
+            keep += [nodes, idx]
+        self._check(self.lib.tracer_upload_scene(self.h, ctypes.byref(d)))
+
+    def set_materials(self, mats: np.ndarray):
+        mats = np.ascontiguousarray(mats, S.MATERIAL)
+        self._check(self.lib.tracer_set_materials(self.h, _ptr(mats), len(mats)))
+
+    @staticmethod
+    def params(width, height, spp=4, max_depth=4, rr_start=0, sky=(0.0, 0.0, 0.0), tie_mode=TIES_STRICT,
+               kernel=KERNEL_AUTO, block=0, stack_depth=0, wavefront=0, aovs=(AOV_RGBA8,), stats=False) -> TraceParams:
+        p = TraceParams()
+        p.width, p.height, p.spp, p.max_depth, p.rr_start = width, height, spp, max_depth, rr_start
+        p.sky = (ctypes.c_float * 3)(*sky)
+        p.tie_mode, p.kernel, p.block, p.stack_depth, p.wavefront = tie_mode, kernel, block, stack_depth, wavefront
+        m = 0
+        for a in aovs:
+            m |= 1 << a
+        p.aov_mask = m
+        p.stats = 1 if stats else 0
+        return p
+
+    def trace(self, frame: np.ndarray, params: TraceParams, stream: int | None = None):
+        f = np.ascontiguousarray(np.asarray(frame, S.FRAME).reshape(()))
+        self._check(self.lib.tracer_trace(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
+                                          ctypes.c_void_p(stream) if stream else None))
+        self.width, self.height = params.width, params.height
+
+    def synchronize(self):
+        self._check(self.lib.tracer_synchronize(self.h))
+
+    def readback(self, aov: int, out: np.ndarray | None = None) -> np.ndarray:
+        w, h = self.width, self.height
+        if aov == AOV_RGBA8:
+            shape, dt = (h, w, 4), np.uint8
+        elif aov == AOV_RGBA32F:
+            shape, dt = (h, w, 4), np.float32
+        elif aov == AOV_PRIMARY_HIT:
+            shape, dt = (h, w, 2), np.uint32
+        elif aov == AOV_STATS:
+            shape, dt = (len(STATS_FIELDS),), np.uint64
+        else:
+            raise ValueError(aov)
+        if out is None:
+            out = np.empty(shape, dt)
+        self._check(self.lib.tracer_readback(self.h, aov, out.ctypes.data_as(ctypes.c_void_p), out.nbytes))
+        return out
+
+    def stats(self) -> dict:
+        v = self.readback(AOV_STATS)
+        return {k: int(x) for k, x in zip(STATS_FIELDS, v)}
+
+    def device_image(self, aov: int):
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self.lib.tracer_device_image(self.h, aov, ctypes.byref(p), ctypes.byref(n)))
+        return p.value, n.value
