@@ -151,7 +151,7 @@ def run_reference(args):
     from vktrace import abi, configs
     import pyoracle
     pyoracle.build()
-    wl = configs.c1()
+    wl = configs.c1(width=args.width, height=args.height, spp=args.spp)
     nodes, idx, _ = abi.build_bvh(2, wl.scene.triangles, leaf_size=4, sah_bins=16)
     threads = os.cpu_count() or 1
     step = 128
@@ -192,15 +192,19 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    wl = configs.c1()
+    wl = configs.c1(width=args.width, height=args.height, spp=args.spp)
     # weak scaling: each rank its own frame (different seed)
     wl.frame["seed"] = np.float32(float(wl.frame["seed"]) + 0.125 * rank)
     nodes, idx, bvh_depth = abi.build_bvh(2, wl.scene.triangles, leaf_size=4, sah_bins=16)
     tr = abi.Tracer(local)
     tr.upload_scene(wl.scene, tri_bvh=(nodes, idx))
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the kernel, the L2 flush and the timing events all
+    # run on it (a legacy-default-stream handle of 0 would mean "the context's
+    # own stream" to the C ABI).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
-    kern = abi.KERNEL_PERSISTENT if args.kernel == "persistent" else abi.KERNEL_PLAIN
+    kern = abi.KERNEL_WAVEFRONT if args.kernel == "wavefront" else abi.KERNEL_PLAIN
     common = dict(spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start, sky=wl.sky, kernel=kern,
                   block=args.block, wavefront=args.wavefront)
     p_count = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=True, **common)
@@ -282,7 +286,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": wl.pixels * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
-                         "kernel": "k_persistent" if kern == abi.KERNEL_PERSISTENT else "k_plain",
+                         "kernel": "wf_extend_bvh" if kern == abi.KERNEL_WAVEFRONT else "k_plain",
                          "algorithmic_bytes_per_launch": ab, "peak_source": peak_kind},
             "clocks": clocks,
             "gpu_launches": args.steps,
@@ -302,10 +306,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--kernel", choices=["persistent", "plain"], default="persistent")
+    ap.add_argument("--kernel", choices=["wavefront", "plain"], default="wavefront")
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--wavefront", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # smaller variants of the workload (profiling captures); defaults = c1
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -173,9 +173,9 @@ typedef struct tracer_scene_desc {
 #define TRACER_TIES_REFERENCE 0 /* Tracer.comp:382/:402/:418 scan-order rule; linear scan only */
 #define TRACER_TIES_STRICT 1    /* nearest (t, primitive id) below tmax; required with a BVH */
 
-#define TRACER_KERNEL_AUTO 0
-#define TRACER_KERNEL_PLAIN 1      /* one thread per pixel, nested sample/bounce loops */
-#define TRACER_KERNEL_PERSISTENT 2 /* persistent warps, per-lane pixel refill */
+#define TRACER_KERNEL_AUTO 0      /* = WAVEFRONT */
+#define TRACER_KERNEL_PLAIN 1     /* one thread per pixel, nested sample/bounce loops */
+#define TRACER_KERNEL_WAVEFRONT 2 /* persistent extend kernel + shade kernel over path queues */
 
 #define TRACER_AOV_RGBA8 0       /* w*h*4 u8: what imageStore writes (Tracer.comp:592) */
 #define TRACER_AOV_RGBA32F 1     /* w*h*4 f32: the colour before UNORM8 conversion */
@@ -195,7 +195,7 @@ typedef struct tracer_trace_params {
     int32_t kernel;         /* TRACER_KERNEL_* */
     uint32_t block;         /* threads per block (multiple of 32, <= 1024); 0 = default */
     uint32_t stack_depth;   /* traversal stack entries per thread; 0 = BVH depth */
-    uint32_t wavefront;     /* persistent kernel: resident CTAs per SM; 0 = occupancy maximum */
+    uint32_t wavefront;     /* wavefront extend kernel: resident CTAs per SM; 0 = occupancy maximum */
     uint32_t aov_mask;      /* bit (1 << TRACER_AOV_*) per image written; 0 = RGBA8 only */
     uint32_t stats;         /* nonzero: count rays, node fetches and primitive tests */
 } tracer_trace_params;
@@ -243,6 +243,19 @@ int tracer_synchronize(tracer_ctx* ctx);
 /* Device address and size of an AOV of the last trace (zero-copy interop;
  * valid until the next trace with a different image size). */
 int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* bytes);
+
+/* Per-kernel GPU time of the last trace, measured with CUDA events when
+ * profiling is on (off by default; the reference has only an FPS counter,
+ * Source/Main.cpp:152-163). */
+typedef struct tracer_timings {
+    float total_ms;     /* whole trace */
+    float extend_ms;    /* wavefront: sum over rounds of the extend (traversal) kernel */
+    float shade_ms;     /* wavefront: sum over rounds of the shade kernel */
+    uint32_t rounds;    /* wavefront rounds (extend + shade) */
+    uint32_t launches;  /* kernels launched */
+} tracer_timings;
+int tracer_set_profiling(tracer_ctx* ctx, int enable);
+int tracer_last_timings(tracer_ctx* ctx, tracer_timings* out);
 
 #ifdef __cplusplus
 }

@@ -13,7 +13,7 @@ from vktrace import scene as S
 
 pytestmark = pytest.mark.gpu
 
-KERNELS = [abi.KERNEL_PLAIN, abi.KERNEL_PERSISTENT]
+KERNELS = [abi.KERNEL_PLAIN, abi.KERNEL_WAVEFRONT]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -25,14 +25,16 @@ def test_reference_scene(gpu_tracer, kernel):
     g = run_gpu(gpu_tracer, sc, fr, 160, 128, 4, 4, tie=abi.TIES_REFERENCE, kernel=kernel)
     o = run_oracle(sc, fr, 160, 128, 4, 4, tie=0)
     r = compare(g, o)
-    assert r["bit_exact_pixels"] > 0.99, r
+    # Paths are identical; remaining differences are last-ulp powf results
+    # (CUDA vs the host C library) in next-event shading and the 1/2.2 gamma.
+    assert r["rmse"] < 1e-6, r
 
 
 def test_reference_scene_full_size(gpu_tracer):
     """Ref: 1024x1024, 4 spp, depth 4 (Source/Main.cpp:112, Tracer.comp:179-180)."""
     sc = S.reference_scene()
     fr = S.reference_frame(0.5)
-    g = run_gpu(gpu_tracer, sc, fr, 1024, 1024, 4, 4, tie=abi.TIES_REFERENCE, kernel=abi.KERNEL_PERSISTENT)
+    g = run_gpu(gpu_tracer, sc, fr, 1024, 1024, 4, 4, tie=abi.TIES_REFERENCE, kernel=abi.KERNEL_WAVEFRONT)
     o = run_oracle(sc, fr, 1024, 1024, 4, 4, tie=0)
     compare(g, o)
 
@@ -64,14 +66,16 @@ def test_triangle_soup_sah(gpu_tracer, kernel):
 
 
 def test_kernels_identical(gpu_tracer):
-    """The plain and persistent kernels compute the same bits."""
+    """The plain and wavefront kernels compute the same bits."""
     sc = soup_scene(2, 2000)
     fr = S.frame(S.look_at((0.0, 5.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.3)
     a = run_gpu(gpu_tracer, sc, fr, 77, 61, 3, 6, rr_start=2, sky=(0.8, 0.9, 1.0), kernel=abi.KERNEL_PLAIN)
-    b = run_gpu(gpu_tracer, sc, fr, 77, 61, 3, 6, rr_start=2, sky=(0.8, 0.9, 1.0), kernel=abi.KERNEL_PERSISTENT)
+    b = run_gpu(gpu_tracer, sc, fr, 77, 61, 3, 6, rr_start=2, sky=(0.8, 0.9, 1.0), kernel=abi.KERNEL_WAVEFRONT)
     assert np.array_equal(a["rgba32f"].view(np.uint32), b["rgba32f"].view(np.uint32))
+    assert np.array_equal(a["rgba8"], b["rgba8"])
     assert np.array_equal(a["hit_id"], b["hit_id"])
-    assert a["stats"] == b["stats"]
+    for k in ("closest_rays", "shadow_rays", "hits"):
+        assert a["stats"][k] == b["stats"][k]
 
 
 def test_bvh_equals_linear_strict(gpu_tracer):

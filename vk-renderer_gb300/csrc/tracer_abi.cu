@@ -78,8 +78,19 @@ struct tracer_ctx {
     DevBuf<uint2> hit;
     DevBuf<unsigned long long> stats;
     DevBuf<int> status;
-    DevBuf<uint32_t> work;
     uint32_t last_mask = 0;
+    // wavefront path state (scratch, one slot per pixel)
+    DevBuf<float4> wf_ray_o, wf_ray_d, wf_acc, wf_mask, wf_accum;
+    DevBuf<uint4> wf_hit;
+    DevBuf<uint32_t> wf_prim0, wf_q0, wf_q1, wf_count;
+    uint32_t* pinned_counts = nullptr;  // lagged queue lengths read by the launch loop
+    std::vector<cudaEvent_t> count_events;
+    // optional per-kernel timing of the last trace
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_events;  // 3 per round: before extend, after extend, after shade
+    cudaEvent_t prof_begin = nullptr, prof_end = nullptr;
+    uint32_t last_rounds = 0, last_launches = 0;
+    int last_kernel = 0;
 };
 
 namespace {
@@ -152,6 +163,47 @@ int finish(tracer_ctx* c)
     return TRACER_OK;
 }
 
+constexpr int kCountSlots = 8;  // ring of lagged queue-length copies
+constexpr int kCountLag = 3;    // rounds the launch loop runs ahead of the GPU
+
+void release_wavefront(tracer_ctx* c)
+{
+    c->wf_ray_o.release();
+    c->wf_ray_d.release();
+    c->wf_acc.release();
+    c->wf_mask.release();
+    c->wf_accum.release();
+    c->wf_hit.release();
+    c->wf_prim0.release();
+    c->wf_q0.release();
+    c->wf_q1.release();
+}
+
+cudaError_t ensure_wavefront(tracer_ctx* c, size_t npx)
+{
+    cudaError_t e = dalloc(c->wf_ray_o, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_ray_d, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_acc, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_mask, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_accum, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_hit, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_prim0, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_q0, npx);
+    if (e == cudaSuccess) e = dalloc(c->wf_q1, npx);
+    if (e != cudaSuccess) release_wavefront(c);
+    return e;
+}
+
+cudaEvent_t prof_event(tracer_ctx* c, size_t i)
+{
+    while (c->prof_events.size() <= i) {
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+        c->prof_events.push_back(ev);
+    }
+    return c->prof_events[i];
+}
+
 // Builds (or validates) one BVH; returns the leaf-order permutation.
 int prepare_bvh(tracer_ctx* c, int kind, int prim_type, const void* prims, uint32_t n, uint32_t leaf, uint32_t bins,
                 const tracer_bvh_node* given, uint32_t n_given, const uint32_t* given_idx,
@@ -216,7 +268,15 @@ int tracer_create(tracer_ctx** out, int cuda_device)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = dalloc(c->stats, C_COUNT);
     if (e == cudaSuccess) e = dalloc(c->status, 1);
-    if (e == cudaSuccess) e = dalloc(c->work, 1);
+    if (e == cudaSuccess) e = dalloc(c->wf_count, 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->pinned_counts, sizeof(uint32_t) * kCountSlots);
+    if (e == cudaSuccess) {
+        c->count_events.resize(kCountSlots, nullptr);
+        for (auto& ev : c->count_events)
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreate(&c->prof_begin);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->prof_end);
     if (e != cudaSuccess) {
         tracer_destroy(c);
         return e == cudaErrorMemoryAllocation ? TRACER_ERR_OOM : TRACER_ERR_CUDA;
@@ -236,7 +296,15 @@ void tracer_destroy(tracer_ctx* c)
     c->hit.release();
     c->stats.release();
     c->status.release();
-    c->work.release();
+    release_wavefront(c);
+    c->wf_count.release();
+    if (c->pinned_counts) cudaFreeHost(c->pinned_counts);
+    for (auto ev : c->count_events)
+        if (ev) cudaEventDestroy(ev);
+    for (auto ev : c->prof_events)
+        if (ev) cudaEventDestroy(ev);
+    if (c->prof_begin) cudaEventDestroy(c->prof_begin);
+    if (c->prof_end) cudaEventDestroy(c->prof_end);
     if (c->done) cudaEventDestroy(c->done);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -364,8 +432,8 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
     if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
         return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
-    int kernel = p->kernel == TRACER_KERNEL_AUTO ? TRACER_KERNEL_PERSISTENT : p->kernel;
-    if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_PERSISTENT)
+    const int kernel = p->kernel == TRACER_KERNEL_AUTO ? TRACER_KERNEL_WAVEFRONT : p->kernel;
+    if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
     uint32_t block = p->block ? p->block : 128;
     if (block % 32 != 0 || block < 32 || block > 256)
@@ -374,8 +442,8 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     uint32_t stack = p->stack_depth ? p->stack_depth : need;
     if (c->scene.bvh && stack < need)
         return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
-    if ((size_t)stack * block * 8 > 200 * 1024)
-        return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u x block %u exceeds shared memory", stack, block);
+    if ((size_t)stack * 256 * 8 > 200 * 1024)
+        return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
     const uint32_t mask = p->aov_mask ? p->aov_mask : (1u << TRACER_AOV_RGBA8);
     if (mask & ~((1u << TRACER_AOV_RGBA8) | (1u << TRACER_AOV_RGBA32F) | (1u << TRACER_AOV_PRIMARY_HIT) |
                  (1u << TRACER_AOV_STATS)))
@@ -421,30 +489,97 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     a.hit = (mask & (1u << TRACER_AOV_PRIMARY_HIT)) ? c->hit.p : nullptr;
     a.stats = c->stats.p;
     a.status = c->status.p;
-    a.work = c->work.p;
-    a.num_pixels = persistent_ids(p->width, p->height);
-
-    LaunchConfig lc;
-    lc.kernel = kernel;
-    lc.block = block;
-    lc.stats = (p->stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
-    lc.tie = p->tie_mode;
-    lc.bvh = s.bvh ? 1 : 0;
-    lc.grid = 0;
-    if (kernel == TRACER_KERNEL_PERSISTENT) {
-        int per = persistent_blocks_per_sm(lc, stack, lc.stats, lc.bvh, lc.tie);
-        if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "persistent kernel cannot be resident with block %u", block);
-        if (p->wavefront && (int)p->wavefront < per) per = (int)p->wavefront;
-        lc.grid = (uint32_t)(per * c->sm_count);
-    }
+    const int stats = (p->stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
+    if (stats) c->last_mask |= 1u << TRACER_AOV_STATS;
     cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
     e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->work.p, 0, sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = launch_trace(a, lc, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "trace set-up");
+    c->last_kernel = kernel;
+    c->last_rounds = 0;
+    c->last_launches = 0;
+    if (c->profiling) cudaEventRecord(c->prof_begin, st);
+
+    if (kernel == TRACER_KERNEL_PLAIN) {
+        LaunchConfig lc{block, stats, p->tie_mode, s.bvh ? 1 : 0};
+        e = launch_plain(a, lc, st);
+        c->last_launches = 1;
+    } else {
+        e = ensure_wavefront(c, npx);
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront state allocation");
+        WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
+                   c->wf_prim0.p, {c->wf_q0.p, c->wf_q1.p}, c->wf_count.p};
+        WfConfig wc;
+        wc.tie = p->tie_mode;
+        wc.bvh = s.bvh ? 1 : 0;
+        wc.stats = stats;
+        int per = wf_extend_blocks_per_sm(stack, wc.bvh, wc.tie, stats);
+        if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "extend kernel cannot be resident (stack %u)", stack);
+        if (p->wavefront && (int)p->wavefront < per) per = (int)p->wavefront;
+        wc.extend_grid = (uint32_t)(per * c->sm_count);
+        const size_t sg = (npx + 255) / 256;
+        wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
+        e = wf_launch_generate(a, ws, st);
+        c->last_launches = 1;
+        // Each round advances every live path by one bounce; no path needs
+        // more than spp * max_depth rounds.  The loop stops once a queue comes
+        // back empty, reading queue lengths a few rounds behind the launches.
+        const uint64_t max_rounds = (uint64_t)p->spp * p->max_depth + 1;
+        for (uint64_t r = 0; r < max_rounds && e == cudaSuccess; ++r) {
+            const int qsel = (int)(r & 1);
+            if (c->profiling) cudaEventRecord(prof_event(c, 3 * r), st);
+            e = wf_launch_extend(a, ws, wc, qsel, st);
+            if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 1), st);
+            if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, qsel, st);
+            if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 2), st);
+            c->last_launches += 2;
+            c->last_rounds = (uint32_t)(r + 1);
+            const int slot = (int)(r % kCountSlots);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(c->pinned_counts + slot, c->wf_count.p + (qsel ^ 1), sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaEventRecord(c->count_events[slot], st);
+            if (e == cudaSuccess && r >= (uint64_t)kCountLag) {
+                const int old = (int)((r - kCountLag) % kCountSlots);
+                int w = wait_event(c, c->count_events[old]);
+                if (w != TRACER_OK) return w;
+                if (c->pinned_counts[old] == 0) break;
+            }
+        }
+    }
+    if (c->profiling) cudaEventRecord(c->prof_end, st);
     if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
     if (e != cudaSuccess) return cuda_fail(c, e, "trace launch");
     c->pending = true;
+    return TRACER_OK;
+}
+
+int tracer_set_profiling(tracer_ctx* c, int enable)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    c->profiling = enable != 0;
+    return TRACER_OK;
+}
+
+int tracer_last_timings(tracer_ctx* c, tracer_timings* out)
+{
+    if (!c || !out) return TRACER_ERR_INVALID_ARG;
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    std::memset(out, 0, sizeof *out);
+    out->rounds = c->last_rounds;
+    out->launches = c->last_launches;
+    if (!c->profiling) return fail(c, TRACER_ERR_INVALID_ARG, "profiling is off (tracer_set_profiling)");
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, c->prof_begin, c->prof_end) == cudaSuccess) out->total_ms = ms;
+    if (c->last_kernel == TRACER_KERNEL_WAVEFRONT) {
+        for (uint32_t i = 0; i < c->last_rounds; ++i) {
+            if (cudaEventElapsedTime(&ms, c->prof_events[3 * i], c->prof_events[3 * i + 1]) == cudaSuccess)
+                out->extend_ms += ms;
+            if (cudaEventElapsedTime(&ms, c->prof_events[3 * i + 1], c->prof_events[3 * i + 2]) == cudaSuccess)
+                out->shade_ms += ms;
+        }
+    }
     return TRACER_OK;
 }
 

@@ -27,8 +27,6 @@ struct TraceArgs {
     uint2* hit;
     unsigned long long* stats;  // C_COUNT counters
     int* status;
-    uint32_t* work;             // persistent kernel: next pixel to hand out
-    uint32_t num_pixels;
 };
 
 // Traversal stack of one thread in shared memory: entry i of thread t at
@@ -314,6 +312,57 @@ __device__ __forceinline__ V3 nee_one(TR& tr, const TraceArgs& a, uint32_t si, V
     return (kD * mat.albedo / PI + specular) * attenuation * NdotL;
 }
 
+// tmax of the closest-hit ray at a depth: 3000 / (depth + 1)^2 (Tracer.comp:444)
+__device__ __forceinline__ float depth_tmax(uint32_t depth)
+{
+    const float dp1 = (float)(depth + 1);
+    return 3000.0f / (dp1 * dp1);
+}
+
+// The part of one depth iteration of radiance (Tracer.comp:445-549) that
+// follows trace_ray: sky on a miss, material scatter with next-event
+// estimation, Russian roulette.  Updates acc, mask and ray; returns false
+// when the path ends (miss or roulette).  acc must already be clamped
+// (Tracer.comp:441; the clamp does not affect the trace, so it may run before
+// or after it).
+template <class TR>
+__device__ __forceinline__ bool shade_bounce(TR& tr, const TraceArgs& a, uint32_t depth, bool found, const Hit& h,
+                                             Ray& ray, V3& acc, V3& mask, Rng& g)
+{
+    if (!found) {
+        if (a.sky_on) acc = acc + mask * a.sky;
+        return false;
+    }
+    V3 P, N;
+    Material mat;
+    tr.surface(ray, h, P, N, mat);
+    if (mat.type == MAT_DIFFUSE) {
+        const float r2 = rand01(g);
+        const V3 d = jitter(N, (2.0f * PI) * rand01(g), sqrtf(r2), sqrtf(1.0f - r2)) * (1.0f - mat.metalness);
+        V3 e = splat(0.0f);
+        for (uint32_t k = 0; k < a.sc.ne; ++k) e = e + nee_one(tr, a, __ldg(a.sc.emit + k), P, N, mat, g);
+        const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
+        const V3 emissive = emits ? normalize(mat.emissive) : splat(0.0f);
+        acc = acc + mask * (emissive + e);
+        mask = mask * mat.albedo;
+        ray = Ray{P, normalize(reflect(ray.d, N) + d)};
+    } else if (mat.type == MAT_DIELECTRIC) {
+        acc = acc + mat.emissive * mask;
+        mask = mask * mat.albedo;
+        const float cosine = -dot(ray.d, N) / length(ray.d);
+        const V3 reflected = reflect(ray.d, N);
+        const V3 refracted = refract(ray.d, N, mat.roughness);
+        const float prob = (refracted == splat(0.0f)) ? 1.0f : schlick(cosine, mat.roughness);
+        ray = Ray{P, normalize(rand01(g) < prob ? reflected : refracted)};
+    }  // other types: the shader's switch has no default; the ray is left as it was
+    if (depth >= a.rr_start) {
+        const float p = max3(mask);
+        if (rand01(g) > p) return false;
+        mask = mask * (1.0f / p);
+    }
+    return true;
+}
+
 // Tracer.comp:433-553 (radiance), extensions: rr_start, sky, max_depth.
 // prim0 / t0 receive the first ray's hit when non-null.
 template <class TR>
@@ -324,44 +373,13 @@ __device__ __forceinline__ V3 radiance(TR& tr, const TraceArgs& a, Ray ray, Rng&
     for (uint32_t depth = 0; depth < a.max_depth; ++depth) {
         acc = vclamp01(acc);
         Hit h;
-        const float dp1 = (float)(depth + 1);
-        h.t = 3000.0f / (dp1 * dp1);
+        h.t = depth_tmax(depth);
         const bool found = tr.trace(ray, h, false);
         if (prim0 && depth == 0) {
             *prim0 = found ? h.prim : NO_PRIM;
             *t0 = found ? h.t : -1.0f;
         }
-        if (!found) {
-            if (a.sky_on) acc = acc + mask * a.sky;
-            break;
-        }
-        V3 P, N;
-        Material mat;
-        tr.surface(ray, h, P, N, mat);
-        if (mat.type == MAT_DIFFUSE) {
-            const float r2 = rand01(g);
-            const V3 d = jitter(N, (2.0f * PI) * rand01(g), sqrtf(r2), sqrtf(1.0f - r2)) * (1.0f - mat.metalness);
-            V3 e = splat(0.0f);
-            for (uint32_t k = 0; k < a.sc.ne; ++k) e = e + nee_one(tr, a, __ldg(a.sc.emit + k), P, N, mat, g);
-            const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
-            const V3 emissive = emits ? normalize(mat.emissive) : splat(0.0f);
-            acc = acc + mask * (emissive + e);
-            mask = mask * mat.albedo;
-            ray = Ray{P, normalize(reflect(ray.d, N) + d)};
-        } else if (mat.type == MAT_DIELECTRIC) {
-            acc = acc + mat.emissive * mask;
-            mask = mask * mat.albedo;
-            const float cosine = -dot(ray.d, N) / length(ray.d);
-            const V3 reflected = reflect(ray.d, N);
-            const V3 refracted = refract(ray.d, N, mat.roughness);
-            const float prob = (refracted == splat(0.0f)) ? 1.0f : schlick(cosine, mat.roughness);
-            ray = Ray{P, normalize(rand01(g) < prob ? reflected : refracted)};
-        }
-        if (depth >= a.rr_start) {
-            const float p = max3(mask);
-            if (rand01(g) > p) break;
-            mask = mask * (1.0f / p);
-        }
+        if (!shade_bounce(tr, a, depth, found, h, ray, acc, mask, g)) break;
     }
     return acc;
 }
@@ -374,13 +392,18 @@ __device__ __forceinline__ unsigned char unorm8(float x)
 }
 
 // Tracer.comp:557-574: RNG seeding and the primary ray of pixel (x, y).
-__device__ __forceinline__ Ray primary_ray(const TraceArgs& a, uint32_t x, uint32_t y, Rng& g)
+__device__ __forceinline__ void seed_rng(const TraceArgs& a, uint32_t x, uint32_t y, Rng& g)
 {
     const float uvx = (float)x / (float)a.width;
     const float uvy = (float)y / (float)a.height;
     g.salt = uvy / uvx + a.fr.seed;
     g.cx = uvx;
     g.cy = uvy;
+}
+__device__ __forceinline__ Ray primary_ray(const TraceArgs& a, uint32_t x, uint32_t y)
+{
+    const float uvx = (float)x / (float)a.width;
+    const float uvy = (float)y / (float)a.height;
     const float tx = 2.0f * uvx - 1.0f;
     const float ty = 2.0f * uvy - 1.0f;
     const V3 dir = (a.fr.cdir + a.fr.cright * tx + a.fr.cup * ty) * v3(a.fr.aspect, 1.0f, a.fr.aspect);

@@ -1,0 +1,504 @@
+// Wavefront path tracing for sm_103a: the radiance loop of Assets/Tracer.comp
+// split into stages that each run as their own kernel over a queue of live
+// paths, one path per pixel.
+//
+//   wf_generate  seeds every pixel's RNG (Tracer.comp:563-566), writes its
+//                primary ray (:568-574) and queues all pixels.
+//   wf_extend    persistent warps trace the queued rays (trace_ray,
+//                :374-431).  Each lane owns one ray at a time and takes the
+//                next ray from the queue as soon as its ray is finished
+//                (warp-aggregated fetch: ballot + popc + one atomicAdd).
+//                BVH traversal is the speculative while-while scheme: all
+//                lanes step through interior nodes together, postponing the
+//                first leaf each finds, then all test their leaves together;
+//                stacks live in shared memory.  Small register footprint, so
+//                many warps per SM hide the L1/L2 latency of node fetches.
+//   wf_shade     one thread per queued path: the rest of the depth iteration
+//                (:441-549: clamp, sky, scatter, next-event estimation, Russian
+//                roulette).  A surviving path appends itself to the next queue
+//                (warp-aggregated atomics = warp-level ray compaction); a
+//                finished sample starts the pixel's next sample, whose RNG
+//                continues where the last one stopped (the shader's rand_salt
+//                runs across samples, :578-581); a finished pixel is resolved
+//                (:585-592).
+//
+// Per pixel the operations are exactly those of the plain kernel, in the same
+// order, so images and hits are identical to it and to the oracle.  Only the
+// order of node visits inside one ray's traversal differs (it depends on the
+// warp), which changes no result under strict ties but does change the node
+// counters.
+
+#include <cuda_runtime.h>
+
+#include "tracer_core.cuh"
+#include "tracer_wavefront.h"
+
+namespace vkt {
+
+__device__ __forceinline__ int leaf_enc(int first, int count) { return -1 - ((first << 6) | (count - 1)); }
+__device__ __forceinline__ void leaf_dec(int enc, int& first, int& count)
+{
+    const int v = -1 - enc;
+    first = v >> 6;
+    count = (v & 63) + 1;
+}
+// Reference to a child record: leaf -> negative code, interior -> index of its
+// children pair (>= 1).
+__device__ __forceinline__ int child_enc(float4 lo, float4 hi)
+{
+    const int cnt = __float_as_int(hi.w);
+    const int left = __float_as_int(lo.w);
+    return cnt > 0 ? leaf_enc(left, cnt) : left;
+}
+
+__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* queue, uint32_t* count)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const unsigned m = __ballot_sync(full, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(full, base, leader);
+    if (want) queue[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// ---------------------------------------------------------------- generate --
+__global__ void __launch_bounds__(256) wf_generate(TraceArgs a, WfState s)
+{
+    const uint32_t n = a.width * a.height;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        s.count[0] = n;
+        s.count[1] = 0;
+        s.count[2] = 0;
+    }
+    if (i >= n) return;
+    const uint32_t x = i % a.width, y = i / a.width;
+    Rng g;
+    seed_rng(a, x, y, g);
+    const Ray r = primary_ray(a, x, y);
+    s.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, depth_tmax(0));
+    s.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, 0.0f);
+    s.acc[i] = make_float4(0.0f, 0.0f, 0.0f, g.salt);
+    s.mask[i] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
+    s.accum[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0u));
+    s.prim0[i] = NO_PRIM;
+    s.queue[0][i] = i;
+}
+
+// ------------------------------------------------------------------ extend --
+template <bool STATS>
+struct Lane {
+    V3 o, d;
+    BoxRay br;
+    float tmax;
+    Hit h;
+    int cur, leaf, sp, pass;
+    uint32_t pid, steps;
+    bool has;
+};
+
+template <int TIE, bool STATS>
+__device__ __forceinline__ void write_hit(const WfState& s, uint32_t pid, const Hit& h)
+{
+    s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+}
+
+// Planes after the BVHs (unbounded; scanned linearly, Tracer.comp:414-428).
+template <int TIE, bool STATS>
+__device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, Hit& h, float tmax, Counters& cnt)
+{
+    for (uint32_t i = 0; i < sc.np; ++i) {
+        if (STATS) cnt.c[C_PLANES]++;
+        const float4 q = __ldg(sc.planes + 4 * (size_t)i + 3);
+        const float tt = plane_intersect(ray, v3(q), q.w);
+        const uint32_t id = sc.nt + sc.ns + i;
+        if (accept<TIE>(tt, id, h, tmax, true)) {
+            h.t = tt;
+            h.prim = id;
+            h.kind = 3;
+            h.slot = i;
+        }
+    }
+}
+
+template <bool STATS>
+__device__ __forceinline__ void start_pass(const DevScene& sc, Lane<STATS>& L, Counters& cnt)
+{
+    const float4* nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
+    const float4 lo = __ldg(nodes), hi = __ldg(nodes + 1);
+    if (STATS) cnt.c[C_NODES]++;
+    float tn;
+    L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? child_enc(lo, hi) : 0;
+    L.leaf = 0;
+    L.sp = 0;
+    if (L.cur < 0) {  // the root is a leaf
+        L.leaf = L.cur;
+        L.cur = 0;
+    }
+}
+
+template <bool STATS>
+__device__ __forceinline__ int pop(Lane<STATS>& L, const Stack& stk)
+{
+    while (L.sp > 0) {
+        --L.sp;
+        const int e = stk.ci[L.sp * stk.stride];
+        const float et = stk.tn[L.sp * stk.stride];
+        if (et <= L.h.t * BOX_SLACK) return e;
+    }
+    return 0;
+}
+
+template <int TIE, bool STATS>
+__global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, int qsel)
+{
+    extern __shared__ int smem[];
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
+                    (int)blockDim.x, (int)a.stack_depth};
+    const DevScene& sc = a.sc;
+    const uint32_t total = s.count[qsel];
+    const uint32_t* queue = s.queue[qsel];
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
+    const bool has_tri = sc.n_tri_nodes > 0 && sc.nt > 0;
+    const bool has_sph = sc.n_sph_nodes > 0 && sc.ns > 0;
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    Lane<STATS> L;
+    L.has = false;
+    bool exhausted = false;
+    for (;;) {
+        // 1) idle lanes take the next rays of the queue
+        const unsigned need = __ballot_sync(full, !L.has && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&s.count[2], (uint32_t)__popc(need));
+            base = __shfl_sync(full, base, leader);
+            if (!L.has && !exhausted) {
+                const uint32_t qi = base + __popc(need & ((1u << lane) - 1u));
+                if (qi >= total) {
+                    exhausted = true;
+                } else {
+                    L.pid = queue[qi];
+                    const float4 ro = s.ray_o[L.pid];
+                    const float4 rd = s.ray_d[L.pid];
+                    L.o = v3(ro);
+                    L.d = v3(rd);
+                    L.tmax = ro.w;
+                    L.h.t = ro.w;
+                    L.h.prim = NO_PRIM;
+                    L.h.kind = 0;
+                    L.h.slot = 0;
+                    L.steps = 0;
+                    if (STATS) cnt.c[C_CLOSEST]++;
+                    L.has = true;
+                    if (isnan3(L.d) || (!has_tri && !has_sph)) {
+                        // no BVH work: NaN directions hit nothing; planes only
+                        if (!isnan3(L.d)) planes_pass<TIE, STATS>(sc, Ray{L.o, L.d}, L.h, L.tmax, cnt);
+                        if (STATS && L.h.kind) cnt.c[C_HITS]++;
+                        write_hit<TIE, STATS>(s, L.pid, L.h);
+                        L.has = false;
+                    } else {
+                        L.br = make_boxray(Ray{L.o, L.d});
+                        L.pass = has_tri ? 0 : 1;
+                        start_pass<STATS>(sc, L, cnt);
+                    }
+                }
+            }
+        }
+        if (!__any_sync(full, L.has)) {
+            if (__all_sync(full, exhausted)) break;
+            continue;
+        }
+        // 2) interior nodes, until every searching lane has found a leaf
+        for (;;) {
+            const bool can = L.has && L.cur > 0;
+            const bool searching = can && L.leaf == 0;
+            if (!__any_sync(full, searching)) break;
+            if (can) {
+                if (++L.steps > a.trav_limit) {
+                    atomicCAS(a.status, ST_OK, ST_TRAVERSAL_LIMIT);
+                    L.cur = 0;
+                    L.leaf = 0;
+                    L.sp = 0;
+                } else {
+                    const float4* nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
+                    const float4* c = nodes + 2 * (size_t)L.cur;
+                    const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
+                    if (STATS) cnt.c[C_NODES] += 2;
+                    float t0, t1;
+                    const bool h0 = box_hit(L.br, lo0, hi0, L.h.t, t0);
+                    const bool h1 = box_hit(L.br, lo1, hi1, L.h.t, t1);
+                    const int e0 = child_enc(lo0, hi0), e1 = child_enc(lo1, hi1);
+                    if (!h0 && !h1) {
+                        L.cur = pop<STATS>(L, stk);
+                    } else {
+                        const bool swap = h1 && (!h0 || t1 < t0);
+                        L.cur = swap ? e1 : e0;
+                        if (h0 && h1) {
+                            if (L.sp >= stk.cap) {
+                                atomicCAS(a.status, ST_OK, ST_STACK_OVERFLOW);
+                            } else {
+                                stk.ci[L.sp * stk.stride] = swap ? e0 : e1;
+                                stk.tn[L.sp * stk.stride] = swap ? t0 : t1;
+                                ++L.sp;
+                            }
+                        }
+                    }
+                    if (L.cur < 0 && L.leaf == 0) {
+                        L.leaf = L.cur;
+                        L.cur = pop<STATS>(L, stk);
+                    }
+                }
+            }
+        }
+        // 3) leaves
+        for (;;) {
+            const bool lf = L.has && L.leaf < 0;
+            if (!__any_sync(full, lf)) break;
+            if (lf) {
+                int first, count;
+                leaf_dec(L.leaf, first, count);
+                const Ray ray{L.o, L.d};
+                if (L.pass == 0) {
+                    for (int k = 0; k < count; ++k) {
+                        if (STATS) cnt.c[C_TRIS]++;
+                        const float4* t = sc.tri + 3 * (size_t)(first + k);
+                        const float4 ta = __ldg(t), tb = __ldg(t + 1), tc = __ldg(t + 2);
+                        const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
+                        const uint32_t id = __float_as_uint(tb.w);
+                        if (accept<TIE>(tt, id, L.h, L.tmax, false)) {
+                            L.h.t = tt;
+                            L.h.prim = id;
+                            L.h.kind = 1;
+                            L.h.slot = first + k;
+                        }
+                    }
+                } else {
+                    for (int k = 0; k < count; ++k) {
+                        if (STATS) cnt.c[C_SPHERES]++;
+                        const float4 gg = __ldg(sc.sph_geo + first + k);
+                        const float tt = sphere_intersect(ray, v3(gg), gg.w);
+                        const uint32_t id = sc.nt + __ldg(sc.sph_id + first + k);
+                        if (accept<TIE>(tt, id, L.h, L.tmax, false)) {
+                            L.h.t = tt;
+                            L.h.prim = id;
+                            L.h.kind = 2;
+                            L.h.slot = first + k;
+                        }
+                    }
+                }
+                if (L.cur < 0) {
+                    L.leaf = L.cur;
+                    L.cur = pop<STATS>(L, stk);
+                } else {
+                    L.leaf = 0;
+                }
+            }
+        }
+        // 4) finished passes: next primitive kind, or planes and the result
+        if (L.has && L.cur == 0 && L.leaf == 0) {
+            if (L.pass == 0 && has_sph) {
+                L.pass = 1;
+                start_pass<STATS>(sc, L, cnt);
+            } else {
+                planes_pass<TIE, STATS>(sc, Ray{L.o, L.d}, L.h, L.tmax, cnt);
+                if (STATS && L.h.kind) cnt.c[C_HITS]++;
+                write_hit<TIE, STATS>(s, L.pid, L.h);
+                L.has = false;
+            }
+        }
+    }
+    if (STATS) flush_counters(a, cnt);
+}
+
+// Linear-scan scenes (the reference's own trace_ray, reference or strict ties):
+// persistent lanes with the same warp-aggregated fetch.
+template <int TIE, bool STATS>
+__global__ void __launch_bounds__(128) wf_extend_linear(TraceArgs a, WfState s, int qsel)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t total = s.count[qsel];
+    const uint32_t* queue = s.queue[qsel];
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    Tracer<TIE, false, STATS> tr{a.sc, Stack{nullptr, nullptr, 0, 0}, cnt, a.status, a.trav_limit};
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&s.count[2], 32u);
+        base = __shfl_sync(full, base, 0);
+        if (base >= total) break;
+        const uint32_t qi = base + lane;
+        if (qi < total) {
+            const uint32_t pid = queue[qi];
+            const float4 ro = s.ray_o[pid];
+            const float4 rd = s.ray_d[pid];
+            Hit h;
+            h.t = ro.w;
+            tr.trace(Ray{v3(ro), v3(rd)}, h, false);
+            s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+        }
+    }
+    if (STATS) flush_counters(a, cnt);
+}
+
+// ------------------------------------------------------------------- shade --
+template <int TIE, bool BVH, bool STATS>
+__global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel)
+{
+    extern __shared__ int smem[];
+    const uint32_t n = s.count[qsel];
+    const uint32_t* queue = s.queue[qsel];
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // extend's fetch cursor for the next round
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    Tracer<TIE, BVH, STATS> tr{a.sc,
+                               Stack{smem + threadIdx.x,
+                                     reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
+                                     (int)blockDim.x, (int)a.stack_depth},
+                               cnt, a.status, a.trav_limit};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t qi = base + threadIdx.x;
+        const bool active = qi < n;
+        bool again = false;
+        uint32_t pid = 0;
+        if (active) {
+            pid = queue[qi];
+            const uint32_t x = pid % a.width, y = pid / a.width;
+            const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
+            const uint4 hr = s.hit[pid];
+            float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
+            uint32_t prim0 = s.prim0[pid];
+            const uint32_t sd = __float_as_uint(accum4.w);
+            uint32_t sample = sd >> 16, depth = sd & 0xFFFFu;
+            Rng g;
+            g.salt = acc4.w;
+            g.cx = (float)x / (float)a.width;
+            g.cy = (float)y / (float)a.height;
+            V3 acc = vclamp01(v3(acc4));
+            V3 mask = v3(mask4);
+            Hit h;
+            h.t = __uint_as_float(hr.x);
+            h.prim = hr.y;
+            h.slot = hr.z;
+            h.kind = (int)hr.w;
+            const bool found = h.kind != 0;
+            float t0 = mask4.w;
+            if (sample == 0 && depth == 0) {
+                prim0 = found ? h.prim : NO_PRIM;
+                t0 = found ? h.t : -1.0f;
+            }
+            Ray ray{v3(ro), v3(rd)};
+            const bool cont = shade_bounce(tr, a, depth, found, h, ray, acc, mask, g);
+            depth++;
+            V3 accum = v3(accum4);
+            if (cont && depth < a.max_depth) {
+                again = true;
+            } else {
+                accum = accum + acc;
+                sample++;
+                depth = 0;
+                if (sample < a.spp) {
+                    ray = primary_ray(a, x, y);
+                    acc = splat(0.0f);
+                    mask = splat(1.0f);
+                    again = true;
+                } else {
+                    resolve_pixel(a, x, y, accum, g, prim0, t0);
+                }
+            }
+            if (again) {
+                s.ray_o[pid] = make_float4(ray.o.x, ray.o.y, ray.o.z, depth_tmax(depth));
+                s.ray_d[pid] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
+                s.acc[pid] = make_float4(acc.x, acc.y, acc.z, g.salt);
+                s.mask[pid] = make_float4(mask.x, mask.y, mask.z, t0);
+                s.accum[pid] = make_float4(accum.x, accum.y, accum.z, __uint_as_float((sample << 16) | depth));
+                s.prim0[pid] = prim0;
+            }
+        }
+        warp_append(again, pid, s.queue[qsel ^ 1], &s.count[qsel ^ 1]);
+    }
+    if (STATS) flush_counters(a, cnt);
+}
+
+// ---------------------------------------------------------------- dispatch --
+template <int TIE, bool BVH, bool STATS>
+static cudaError_t extend_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    if (BVH) {
+        auto k = wf_extend_bvh<TIE, STATS>;
+        const size_t smem = (size_t)a.stack_depth * 128 * 8;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<c.extend_grid, 128, smem, st>>>(a, s, qsel);
+    } else {
+        wf_extend_linear<TIE, STATS><<<c.extend_grid, 128, 0, st>>>(a, s, qsel);
+    }
+    return cudaGetLastError();
+}
+
+template <int TIE, bool BVH, bool STATS>
+static cudaError_t shade_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    auto k = wf_shade<TIE, BVH, STATS>;
+    const size_t smem = (BVH && a.sc.ne) ? (size_t)a.stack_depth * 256 * 8 : 0;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<c.shade_grid, 256, smem, st>>>(a, s, qsel);
+    return cudaGetLastError();
+}
+
+#define WF_DISPATCH(fn)                                                                                   \
+    if (c.tie == TIE_REFERENCE)                                                                           \
+        return c.stats ? fn<TIE_REFERENCE, false, true>(a, s, c, qsel, st)                                \
+                       : fn<TIE_REFERENCE, false, false>(a, s, c, qsel, st);                              \
+    if (c.bvh)                                                                                            \
+        return c.stats ? fn<TIE_STRICT, true, true>(a, s, c, qsel, st) : fn<TIE_STRICT, true, false>(a, s, c, qsel, st); \
+    return c.stats ? fn<TIE_STRICT, false, true>(a, s, c, qsel, st) : fn<TIE_STRICT, false, false>(a, s, c, qsel, st);
+
+cudaError_t wf_launch_generate(const TraceArgs& a, const WfState& s, cudaStream_t st)
+{
+    const uint32_t n = a.width * a.height;
+    wf_generate<<<(n + 255) / 256, 256, 0, st>>>(a, s);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_launch_extend(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    WF_DISPATCH(extend_t)
+}
+
+cudaError_t wf_launch_shade(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    WF_DISPATCH(shade_t)
+}
+
+int wf_extend_blocks_per_sm(uint32_t stack_depth, int bvh, int tie, int stats)
+{
+    int n = 0;
+    const size_t smem = (size_t)stack_depth * 128 * 8;
+    cudaError_t e;
+    if (bvh) {
+        auto k = stats ? wf_extend_bvh<TIE_STRICT, true> : wf_extend_bvh<TIE_STRICT, false>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, smem);
+    } else if (tie == TIE_REFERENCE) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, stats ? wf_extend_linear<TIE_REFERENCE, true> : wf_extend_linear<TIE_REFERENCE, false>, 128, 0);
+    } else {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, stats ? wf_extend_linear<TIE_STRICT, true> : wf_extend_linear<TIE_STRICT, false>, 128, 0);
+    }
+    return e == cudaSuccess ? n : 0;
+}
+
+}  // namespace vkt

@@ -29,8 +29,8 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall"]
 
-SOURCES = ["tracer_kernels.cu", "tracer_abi.cu", "bvh_build.cpp"]
-HEADERS = ["tracer_device.cuh", "tracer_core.cuh", "tracer_launch.h"]
+SOURCES = ["tracer_kernels.cu", "tracer_wavefront.cu", "tracer_abi.cu", "bvh_build.cpp"]
+HEADERS = ["tracer_device.cuh", "tracer_core.cuh", "tracer_launch.h", "tracer_wavefront.h"]
 
 
 def _nvcc() -> str:

@@ -28,7 +28,7 @@ ERR_NO_SCENE = -10
 ERR_BAD_BVH = -11
 
 TIES_REFERENCE, TIES_STRICT = 0, 1
-KERNEL_AUTO, KERNEL_PLAIN, KERNEL_PERSISTENT = 0, 1, 2
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_WAVEFRONT = 0, 1, 2
 AOV_RGBA8, AOV_RGBA32F, AOV_PRIMARY_HIT, AOV_STATS = 0, 1, 2, 3
 PRIM_TRIANGLE, PRIM_SPHERE = 0, 1
 
@@ -37,7 +37,8 @@ STATS_FIELDS = ["closest_rays", "shadow_rays", "node_fetches", "tri_tests", "sph
 EXPORTED_SYMBOLS = [
     "tracer_create", "tracer_destroy", "tracer_last_error", "tracer_status_string", "tracer_set_timeout",
     "tracer_upload_scene", "tracer_set_materials", "tracer_trace", "tracer_readback", "tracer_synchronize",
-    "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh",
+    "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh", "tracer_set_profiling",
+    "tracer_last_timings",
 ]
 
 
@@ -70,6 +71,11 @@ class TraceParams(ctypes.Structure):
     ]
 
 
+class Timings(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_float), ("extend_ms", ctypes.c_float), ("shade_ms", ctypes.c_float),
+                ("rounds", ctypes.c_uint32), ("launches", ctypes.c_uint32)]
+
+
 _lib = None
 
 
@@ -99,6 +105,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_device_image.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(sz)]
     lib.tracer_build_bvh.argtypes = [i32, i32, vp, u32, u32, u32, vp, ctypes.POINTER(u32), vp, ctypes.POINTER(u32)]
     lib.tracer_validate_bvh.argtypes = [i32, vp, u32, vp, u32, vp, ctypes.POINTER(u32)]
+    lib.tracer_set_profiling.argtypes = [vp, i32]
+    lib.tracer_last_timings.argtypes = [vp, ctypes.POINTER(Timings)]
     if path is None:
         _lib = lib
     return lib
@@ -235,6 +243,14 @@ class Tracer:
     def stats(self) -> dict:
         v = self.readback(AOV_STATS)
         return {k: int(x) for k, x in zip(STATS_FIELDS, v)}
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.tracer_set_profiling(self.h, 1 if on else 0))
+
+    def timings(self) -> dict:
+        t = Timings()
+        self._check(self.lib.tracer_last_timings(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Timings._fields_}
 
     def device_image(self, aov: int):
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
