@@ -257,6 +257,39 @@ typedef struct tracer_timings {
 int tracer_set_profiling(tracer_ctx* ctx, int enable);
 int tracer_last_timings(tracer_ctx* ctx, tracer_timings* out);
 
+/* Trace that allocates no memory during the call.  No counterpart in the
+ * reference (its Vulkan device allocates all its buffers up front in
+ * GraphicsDevice::Construct).
+ *
+ * For callers that must not allocate device memory while rendering: a frame
+ * loop with a fixed time budget, where a cudaMalloc/cudaFree can synchronize
+ * the whole device and stall the frame, or a host engine that owns every
+ * device allocation through its own pool and hands libraries only buffers it
+ * has already allocated.  Such a caller creates the context and uploads the
+ * scene once at start-up, then calls this entry point per frame.
+ *
+ * It runs the wavefront kernels on the scene uploaded to ctx and writes the
+ * image straight into caller-owned device buffers: rgba8_out (w*h*4 bytes)
+ * and/or rgba32f_out (w*h*16 bytes); either may be NULL, not both.  The
+ * wavefront's path state, queues and counters live in one fixed array of
+ * device memory inside the library (about 1.8 MB, reserved on every GPU that
+ * loads the library until the process exits), so images are limited to
+ * TRACER_NOALLOC_MAX_PIXELS pixels and spp * max_depth to
+ * TRACER_NOALLOC_MAX_ROUNDS; larger requests return
+ * TRACER_ERR_NO_SUITABLE_SURFACE / TRACER_ERR_INVALID_ARG with a message.
+ * The first call on a device looks up that array's device address, so make
+ * the first call on each device before any stream capture.  All calls share
+ * the one array and each leaves its contents behind (the kernels clear what
+ * must start at zero); calls that may overlap on the GPU -- on different
+ * streams, or on several contexts of one device -- race on it and must be
+ * ordered by the caller.  Asynchronous on cuda_stream (NULL = the context's
+ * stream); the traversal status words are not read back (with a validated
+ * BVH they cannot trip). */
+#define TRACER_NOALLOC_MAX_PIXELS 16384u /* e.g. 128 x 128 */
+#define TRACER_NOALLOC_MAX_ROUNDS 8192u  /* spp * max_depth */
+int tracer_trace_noalloc(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
+                         void* rgba8_out, void* rgba32f_out, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -631,3 +632,142 @@ int tracer_device_image(tracer_ctx* c, int aov, void** ptr, size_t* bytes)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- no-alloc entry point
+// Scratch of tracer_trace_noalloc: the wavefront path state, both queues, the
+// queue counters and the status/statistics words for up to
+// TRACER_NOALLOC_MAX_PIXELS pixels, in one fixed array so that the call never
+// allocates.  Region sizes are multiples of 256 bytes, so each region stays
+// 256-byte aligned.
+namespace {
+constexpr size_t kNaPix = TRACER_NOALLOC_MAX_PIXELS;
+constexpr size_t kNaF4 = kNaPix * sizeof(float4);   // one float4 / uint4 per pixel
+constexpr size_t kNaU32 = kNaPix * sizeof(uint32_t);
+constexpr size_t kNaOffRayO = 0;
+constexpr size_t kNaOffRayD = kNaOffRayO + kNaF4;
+constexpr size_t kNaOffHit = kNaOffRayD + kNaF4;
+constexpr size_t kNaOffAcc = kNaOffHit + kNaF4;
+constexpr size_t kNaOffMask = kNaOffAcc + kNaF4;
+constexpr size_t kNaOffAccum = kNaOffMask + kNaF4;
+constexpr size_t kNaOffPrim0 = kNaOffAccum + kNaF4;
+constexpr size_t kNaOffQ0 = kNaOffPrim0 + kNaU32;
+constexpr size_t kNaOffQ1 = kNaOffQ0 + kNaU32;
+constexpr size_t kNaOffCount = kNaOffQ1 + kNaU32;     // 4 x u32
+constexpr size_t kNaOffStats = kNaOffCount + 256;     // C_COUNT x u64
+constexpr size_t kNaOffStatus = kNaOffStats + 256;    // int
+constexpr size_t kNaBytes = kNaOffStatus + 256;
+static_assert(kNaF4 % 256 == 0 && kNaU32 % 256 == 0, "regions must keep 256-byte alignment");
+static_assert(C_COUNT * sizeof(unsigned long long) <= 256, "statistics region too small");
+constexpr int kNaMaxDevices = 64;
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kNaMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is only a stand-in for it).
+static int noalloc_scratch(tracer_ctx* c, unsigned char** out)
+{
+    if (c->device < 0 || c->device >= kNaMaxDevices)
+        return fail(c, TRACER_ERR_NO_SUITABLE_GPU, "device %d beyond the no-alloc set-up table", c->device);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[c->device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(c, e, "looking up the no-alloc scratch address");
+        g_noalloc_addr[c->device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[c->device]);
+    return TRACER_OK;
+}
+
+extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params* p,
+                                    void* rgba8_out, void* rgba32f_out, void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!f || !p) return fail(c, TRACER_ERR_INVALID_ARG, "null frame or params");
+    if (!rgba8_out && !rgba32f_out) return fail(c, TRACER_ERR_INVALID_ARG, "no output buffer given");
+    if (!c->scene.loaded) return fail(c, TRACER_ERR_NO_SCENE, "no scene uploaded");
+    if (p->width == 0 || p->height == 0 || (uint64_t)p->width * p->height > kNaPix)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE,
+                    "image %ux%u exceeds the no-alloc limit of %u pixels (use tracer_trace)", p->width, p->height,
+                    TRACER_NOALLOC_MAX_PIXELS);
+    if (p->spp == 0 || p->max_depth == 0 || (uint64_t)p->spp * p->max_depth > TRACER_NOALLOC_MAX_ROUNDS)
+        return fail(c, TRACER_ERR_INVALID_ARG, "spp %u x max_depth %u exceeds the no-alloc limit of %u rounds",
+                    p->spp, p->max_depth, TRACER_NOALLOC_MAX_ROUNDS);
+    if (p->tie_mode != TRACER_TIES_REFERENCE && p->tie_mode != TRACER_TIES_STRICT)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
+    if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
+        return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
+    const SceneBuffers& s = c->scene;
+    const uint32_t need = s.bvh ? (s.depth > 1 ? s.depth : 1) : 0;
+    const uint32_t stack = p->stack_depth ? p->stack_depth : need;
+    if (s.bvh && stack < need)
+        return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
+    if ((size_t)stack * 256 * 8 > 200 * 1024)
+        return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, TRACER_ERR_CUDA, "cannot select device %d", c->device);
+    unsigned char* base = nullptr;
+    int r = noalloc_scratch(c, &base);
+    if (r != TRACER_OK) return r;
+
+    TraceArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
+                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes};
+    a.fr.aspect = f->aspect_ratio;
+    a.fr.seed = f->seed;
+    a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
+    a.fr.cdir = V3{f->camera.dir[0], f->camera.dir[1], f->camera.dir[2]};
+    a.fr.cright = V3{f->camera.right[0], f->camera.right[1], f->camera.right[2]};
+    a.fr.cup = V3{f->camera.up[0], f->camera.up[1], f->camera.up[2]};
+    a.width = p->width;
+    a.height = p->height;
+    a.spp = p->spp;
+    a.max_depth = p->max_depth;
+    a.rr_start = p->rr_start;
+    a.sky = V3{p->sky[0], p->sky[1], p->sky[2]};
+    a.sky_on = !(p->sky[0] == 0.0f && p->sky[1] == 0.0f && p->sky[2] == 0.0f);
+    a.stack_depth = stack;
+    const uint32_t nn = s.n_tri_nodes > s.n_sph_nodes ? s.n_tri_nodes : s.n_sph_nodes;
+    a.trav_limit = 2 * nn + 16;
+    a.rgba8 = static_cast<uchar4*>(rgba8_out);
+    a.rgba32f = static_cast<float4*>(rgba32f_out);
+    a.hit = nullptr;
+    a.stats = reinterpret_cast<unsigned long long*>(base + kNaOffStats);
+    a.status = reinterpret_cast<int*>(base + kNaOffStatus);
+
+    WfState ws{reinterpret_cast<float4*>(base + kNaOffRayO), reinterpret_cast<float4*>(base + kNaOffRayD),
+               reinterpret_cast<uint4*>(base + kNaOffHit), reinterpret_cast<float4*>(base + kNaOffAcc),
+               reinterpret_cast<float4*>(base + kNaOffMask), reinterpret_cast<float4*>(base + kNaOffAccum),
+               reinterpret_cast<uint32_t*>(base + kNaOffPrim0),
+               {reinterpret_cast<uint32_t*>(base + kNaOffQ0), reinterpret_cast<uint32_t*>(base + kNaOffQ1)},
+               reinterpret_cast<uint32_t*>(base + kNaOffCount)};
+    WfConfig wc;
+    wc.tie = p->tie_mode;
+    wc.bvh = s.bvh ? 1 : 0;
+    wc.stats = 0;
+    int per = wf_extend_blocks_per_sm(stack, wc.bvh, wc.tie, 0);
+    if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "extend kernel cannot be resident (stack %u)", stack);
+    if (p->wavefront && (int)p->wavefront < per) per = (int)p->wavefront;
+    wc.extend_grid = (uint32_t)(per * c->sm_count);
+    const size_t npx = (size_t)p->width * p->height;
+    wc.shade_grid = (uint32_t)((npx + 255) / 256);
+
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    // The status word starts at zero; the generate kernel resets the queue
+    // counters; statistics are not collected here.
+    cudaError_t e = cudaMemsetAsync(a.status, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = wf_launch_generate(a, ws, st);
+    // Every round is launched (no queue length is read back to the host); a
+    // round with an empty queue returns at once.
+    const uint32_t rounds = p->spp * p->max_depth + 1;
+    for (uint32_t k = 0; k < rounds && e == cudaSuccess; ++k) {
+        e = wf_launch_extend(a, ws, wc, (int)(k & 1), st);
+        if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, (int)(k & 1), st);
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "no-alloc trace launch");
+    return TRACER_OK;
+}

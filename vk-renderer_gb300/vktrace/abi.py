@@ -38,8 +38,10 @@ EXPORTED_SYMBOLS = [
     "tracer_create", "tracer_destroy", "tracer_last_error", "tracer_status_string", "tracer_set_timeout",
     "tracer_upload_scene", "tracer_set_materials", "tracer_trace", "tracer_readback", "tracer_synchronize",
     "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh", "tracer_set_profiling",
-    "tracer_last_timings",
+    "tracer_last_timings", "tracer_trace_noalloc",
 ]
+NOALLOC_MAX_PIXELS = 16384
+NOALLOC_MAX_ROUNDS = 8192
 
 
 class TracerError(RuntimeError):
@@ -107,6 +109,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_validate_bvh.argtypes = [i32, vp, u32, vp, u32, vp, ctypes.POINTER(u32)]
     lib.tracer_set_profiling.argtypes = [vp, i32]
     lib.tracer_last_timings.argtypes = [vp, ctypes.POINTER(Timings)]
+    lib.tracer_trace_noalloc.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp, vp, vp]
     if path is None:
         _lib = lib
     return lib
@@ -219,6 +222,16 @@ class Tracer:
         self._check(self.lib.tracer_trace(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
                                           ctypes.c_void_p(stream) if stream else None))
         self.width, self.height = params.width, params.height
+
+    def trace_noalloc(self, frame: np.ndarray, params: TraceParams, rgba8_dev: int | None,
+                      rgba32f_dev: int | None, stream: int | None = None):
+        """tracer_trace_noalloc: writes into caller-owned device buffers
+        (addresses as ints) and allocates nothing; asynchronous."""
+        f = np.ascontiguousarray(np.asarray(frame, S.FRAME).reshape(()))
+        self._check(self.lib.tracer_trace_noalloc(
+            self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
+            ctypes.c_void_p(rgba8_dev) if rgba8_dev else None, ctypes.c_void_p(rgba32f_dev) if rgba32f_dev else None,
+            ctypes.c_void_p(stream) if stream else None))
 
     def synchronize(self):
         self._check(self.lib.tracer_synchronize(self.h))
