@@ -38,10 +38,11 @@ METRIC = "Mrays/s on 1 GB300 (fwd, adjoint, batched) at ≤1e-3 RMSE vs plain tr
 UNIT = "Mrays/s"
 L2_FLUSH_BYTES = 256 << 20
 
-# Per-launch DRAM traffic of k_persistent on this workload, from
-# profiles/k_persistent_c1.md (ncu dram__bytes_read.sum + dram__bytes_write.sum);
-# None until captured.
-NCU_TRAFFIC_BYTES = None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ray of the
+# extend kernel, from one ncu capture of every extend launch of the c1 scene
+# at 640x360x4 spp (profiles/wf_extend_bvh_c1_small.md); traffic grows with
+# the number of rays, so the frame's traffic is this times its rays.
+NCU_EXTEND_DRAM_BYTES_PER_RAY = 113.1
 
 
 def peaks():
@@ -207,9 +208,13 @@ def run_ours(args):
     kern = abi.KERNEL_WAVEFRONT if args.kernel == "wavefront" else abi.KERNEL_PLAIN
     common = dict(spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start, sky=wl.sky, kernel=kern,
                   block=args.block, wavefront=args.wavefront)
-    p_count = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=True, **common)
     p_run = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=False, **common)
-    # counting pass (untimed): the kernel is deterministic, every step does this work
+    # counting pass (untimed) with the plain kernel, whose node-visiting order
+    # is the oracle's: the canonical ray / node / primitive counts of the frame.
+    # Every kernel traces exactly these rays (the wavefront's speculative
+    # traversal fetches ~1.5 % more nodes than this canonical count).
+    p_count = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=True,
+                                **dict(common, kernel=abi.KERNEL_PLAIN, block=0))
     tr.trace(wl.frame, p_count, sptr)
     st = tr.stats()
     rays = st["closest_rays"] + st["shadow_rays"]
@@ -245,6 +250,14 @@ def run_ours(args):
         ms = float(t.item())
     value = world * rays / (ms / 1e3) / 1e6
 
+    # per-kernel breakdown of one frame (untimed run with CUDA events around
+    # every extend and shade launch)
+    tr.set_profiling(True)
+    flush.zero_()
+    tr.trace(wl.frame, p_run, sptr)
+    breakdown = tr.timings()
+    tr.set_profiling(False)
+
     # end to end through the C ABI with host buffers
     pinned = torch.empty((wl.height, wl.width, 4), dtype=torch.uint8, pin_memory=True)
     img = pinned.numpy()
@@ -269,7 +282,15 @@ def run_ours(args):
     if rank == 0:
         peak, peak_kind = peaks()
         ab = algorithmic_bytes(st, wl.pixels, 4)
-        achieved = ab / (ms / 1e3) / 1e9
+        # dominant kernel: the traversal (extend) kernel of the wavefront, one
+        # launch per round; its algorithmic bytes are the traversal bytes of
+        # the frame, its time the sum of its launches (CUDA events)
+        if kern == abi.KERNEL_WAVEFRONT and breakdown["extend_ms"] > 0:
+            k_ms = breakdown["extend_ms"]
+            k_bytes = ab - 4 * wl.pixels
+        else:
+            k_ms, k_bytes = ms, ab
+        achieved = k_bytes / (k_ms / 1e3) / 1e9
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -285,11 +306,17 @@ def run_ours(args):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 96,
                     "d2h_bytes_per_step": wl.pixels * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
+                         "frac": achieved / peak,
+                         "traffic": (NCU_EXTEND_DRAM_BYTES_PER_RAY * rays
+                                     if kern == abi.KERNEL_WAVEFRONT else None),
                          "kernel": "wf_extend_bvh" if kern == abi.KERNEL_WAVEFRONT else "k_plain",
-                         "algorithmic_bytes_per_launch": ab, "peak_source": peak_kind},
+                         "algorithmic_bytes_per_frame": k_bytes, "kernel_ms_per_frame": k_ms,
+                         "launches_per_frame": breakdown["rounds"] if kern == abi.KERNEL_WAVEFRONT else 1,
+                         "peak_source": peak_kind,
+                         "note": "scene is L2-resident; algorithmic bytes are served mostly by L1/L2"},
+            "breakdown": breakdown,
             "clocks": clocks,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * int(breakdown["launches"]),
         }
         if world == 1 and not args.no_cpu_baseline:
             v, cores, sample = cpu_baseline_sample(wl, (nodes, idx))

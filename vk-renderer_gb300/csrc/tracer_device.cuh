@@ -275,14 +275,34 @@ __device__ __forceinline__ BoxRay make_boxray(const Ray& r)
     b.nz = -(r.o.z * b.iz);
     return b;
 }
-// Node record = 2 x float4: (bmin, left_or_first) (bmax, count)
+// Three-input IEEE minNum / maxNum (one instruction on sm_100+).  Without NaN
+// inputs they equal the pairwise fminf/fmaxf chains of the definition, up to
+// the sign of a zero result, which no comparison below can see.
+__device__ __forceinline__ float fmin3(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Node record = 2 x float4: (bmin, left_or_first) (bmax, count).  Definition
+// (shared with the oracle): tmin = max(max(min(x0,x1), min(y0,y1)),
+// max(min(z0,z1), 0)), tmax = min(min(max(x0,x1), max(y0,y1)),
+// min(max(z0,z1), tbest)); hit iff tmin <= tmax * (1 + 2^-20).  Rays with a
+// NaN direction never reach this test.
 __device__ __forceinline__ bool box_hit(const BoxRay& r, float4 lo, float4 hi, float tbest, float& tnear)
 {
     float x0 = __fmaf_rn(lo.x, r.ix, r.nx), x1 = __fmaf_rn(hi.x, r.ix, r.nx);
     float y0 = __fmaf_rn(lo.y, r.iy, r.ny), y1 = __fmaf_rn(hi.y, r.iy, r.ny);
     float z0 = __fmaf_rn(lo.z, r.iz, r.nz), z1 = __fmaf_rn(hi.z, r.iz, r.nz);
-    float tmin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
-    float tmax = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tbest));
+    float tmin = fmaxf(fmax3(fminf(x0, x1), fminf(y0, y1), fminf(z0, z1)), 0.0f);
+    float tmax = fminf(fmin3(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1)), tbest);
     tnear = tmin;
     return tmin <= tmax * BOX_SLACK;
 }

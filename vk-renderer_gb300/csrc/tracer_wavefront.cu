@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                     (int)blockDim.x, (int)a.stack_depth};
     const DevScene& sc = a.sc;
     const uint32_t total = s.count[qsel];
-    const uint32_t* queue = s.queue[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
     const bool has_tri = sc.n_tri_nodes > 0 && sc.nt > 0;
     const bool has_sph = sc.n_sph_nodes > 0 && sc.ns > 0;
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(128) wf_extend_linear(TraceArgs a, WfState s, 
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const uint32_t total = s.count[qsel];
-    const uint32_t* queue = s.queue[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
     Counters cnt;
 #pragma unroll
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
 {
     extern __shared__ int smem[];
     const uint32_t n = s.count[qsel];
-    const uint32_t* queue = s.queue[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // extend's fetch cursor for the next round
     Counters cnt;
 #pragma unroll
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
                 s.prim0[pid] = prim0;
             }
         }
-        warp_append(again, pid, s.queue[qsel ^ 1], &s.count[qsel ^ 1]);
+        warp_append(again, pid, qsel ? s.queue[0] : s.queue[1], &s.count[qsel ^ 1]);
     }
     if (STATS) flush_counters(a, cnt);
 }
