@@ -143,6 +143,74 @@ def cpu_baseline_sample(wl, tri_bvh, seconds_target: float = 15.0):
                                      f"{wl.spp} spp), {dt:.1f} s, {rays} rays"
 
 
+def batched_section(local: int, steps: int, warmup: int) -> dict:
+    """c2: 64 scenes (triangles log-uniform in [1k, 200k], c1 geometry,
+    resolutions from {128^2 .. 1024^2}, 4 spp, depth 6) traced (a) by the plain
+    kernel launched once per scene and (b) as one wavefront over all scenes
+    replayed as one CUDA graph, with the launch shape picked by the autotuner.
+    Mrays/s from canonical ray counts; L2 flushed before every timed step."""
+    import numpy as np
+    import torch
+    from vktrace import abi, configs, tune
+    wls = configs.c2()
+    tr = abi.Tracer(local)
+    tr.upload_scenes([w.scene for w in wls])
+    frames = [w.frame for w in wls]
+
+    def prm(kernel, stats=False, aovs=(abi.AOV_RGBA8,)):
+        return [abi.Tracer.params(w.width, w.height, spp=w.spp, max_depth=w.max_depth, rr_start=w.rr_start,
+                                  sky=w.sky, kernel=kernel, aovs=aovs, stats=stats) for w in wls]
+
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    tr.trace_batched(frames, prm(abi.KERNEL_PLAIN, stats=True), use_graph=False, stream=sptr)
+    st = {k: int(v) for k, v in zip(abi.STATS_FIELDS, tr.readback_scene(0, abi.AOV_STATS))}
+    rays = st["closest_rays"] + st["shadow_rays"]
+
+    def timed(params, use_graph):
+        for _ in range(warmup):
+            flush.zero_()
+            tr.trace_batched(frames, params, use_graph=use_graph, stream=sptr)
+        tr.synchronize()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            tr.trace_batched(frames, params, use_graph=use_graph, stream=sptr)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        tr.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs) / steps
+
+    p_plain = prm(abi.KERNEL_PLAIN, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F))
+    ms_plain = timed(p_plain, False)
+    plain_imgs = [tr.readback_scene(k, abi.AOV_RGBA32F) for k in range(len(wls))]
+    p_wf = prm(abi.KERNEL_WAVEFRONT, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F))
+    best, table = tune.autotune_batched(tr, frames, p_wf, budget_s=40.0)
+    for p in p_wf:
+        p.block, p.stack_depth, p.wavefront = best["block"], best["stack_depth"], best["wavefront"]
+    ms_wf = timed(p_wf, True)
+    rmse = 0.0
+    for k in range(len(wls)):
+        a = tr.readback_scene(k, abi.AOV_RGBA32F)[:, 1:, :3].astype(np.float64)
+        b = plain_imgs[k][:, 1:, :3].astype(np.float64)
+        rmse = max(rmse, float(np.sqrt(np.mean((a - b) ** 2))))
+    tr.close()
+    pixels = sum(w.pixels for w in wls)
+    return {"metric": "batched Mrays/s (64 scenes, one CUDA-graph wavefront)", "value": rays / (ms_wf / 1e3) / 1e6,
+            "unit": UNIT, "ms_per_step": ms_wf,
+            "plain_per_scene": {"value": rays / (ms_plain / 1e3) / 1e6, "ms_per_step": ms_plain,
+                                "kernel": "k_plain, one launch per scene"},
+            "speedup_vs_plain_per_scene": ms_plain / ms_wf,
+            "max_image_rmse_vs_plain": rmse, "rays_per_step": rays, "scenes": len(wls), "pixels": pixels,
+            "triangles": int(sum(len(w.scene.triangles) for w in wls)),
+            "autotuned": best, "autotune_candidates": len(table),
+            "config": {"workload": "c2-64scenes-tris-loguniform-1k-200k-res128-1024-4spp-d6-rr3-sah16",
+                       "l2": "flushed before each timed step (256 MiB write)"}}
+
+
 def run_reference(args):
     """CPU restatement of the reference shader (oracle port, same BVH), timed
     on the host cores.  Rank 0 alone works under torchrun."""
@@ -321,6 +389,8 @@ def run_ours(args):
         if world == 1 and not args.no_cpu_baseline:
             v, cores, sample = cpu_baseline_sample(wl, (nodes, idx))
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        if world == 1 and not args.no_batched:
+            line["batched"] = batched_section(local, max(3, args.steps // 2), 2)
         print(json.dumps(line), flush=True)
     tr.close()
     if world > 1:
@@ -337,6 +407,7 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--wavefront", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched section")
     # smaller variants of the workload (profiling captures); defaults = c1
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)

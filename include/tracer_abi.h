@@ -244,6 +244,33 @@ int tracer_synchronize(tracer_ctx* ctx);
  * valid until the next trace with a different image size). */
 int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* bytes);
 
+/* ------------------------------------------------------------ batches
+ * Many independent scenes of uneven size and resolution traced together (no
+ * counterpart in the reference, which renders one fixed scene).  The scenes'
+ * triangles, BVHs, materials, spheres and planes are packed into one device
+ * arena; all scenes' paths share the wavefront queues, so small scenes fill
+ * the GPU together instead of one under-filled launch each. */
+
+/* Uploads n scenes into the context's batch arena (replacing any previous
+ * batch; the single-scene state of tracer_upload_scene is separate).  BVHs
+ * are built per scene on host threads.  Batches need a BVH (bvh != NONE). */
+int tracer_upload_scenes(tracer_ctx* ctx, const tracer_scene_desc* descs, uint32_t n);
+
+/* Traces every scene of the batch: frames[i] and params[i] describe scene i
+ * (image size, spp, depth, RR start, sky; strict ties).  kernel, block,
+ * stack_depth, wavefront, aov_mask and stats are taken from params[0].
+ *   kernel = WAVEFRONT: one wavefront over all scenes.  use_graph != 0 runs
+ *     it as one CUDA graph (generate + every round, captured once per batch
+ *     shape and replayed), so the host neither launches per round nor waits.
+ *   kernel = PLAIN: the plain kernel launched once per scene, in order (the
+ *     per-scene baseline).
+ * Asynchronous on cuda_stream like tracer_trace. */
+int tracer_trace_batched(tracer_ctx* ctx, const tracer_frame* frames, const tracer_trace_params* params, uint32_t n,
+                         int use_graph, void* cuda_stream);
+
+/* Like tracer_readback, for scene `scene` of the last batched trace. */
+int tracer_readback_scene(tracer_ctx* ctx, uint32_t scene, int aov, void* host_dst, size_t bytes);
+
 /* Per-kernel GPU time of the last trace, measured with CUDA events when
  * profiling is on (off by default; the reference has only an FPS counter,
  * Source/Main.cpp:152-163). */

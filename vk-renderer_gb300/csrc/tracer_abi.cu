@@ -13,6 +13,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -83,7 +85,7 @@ struct tracer_ctx {
     // wavefront path state (scratch, one slot per pixel)
     DevBuf<float4> wf_ray_o, wf_ray_d, wf_acc, wf_mask, wf_accum;
     DevBuf<uint4> wf_hit;
-    DevBuf<uint32_t> wf_prim0, wf_q0, wf_q1, wf_count;
+    DevBuf<uint32_t> wf_prim0, wf_q0, wf_q1, wf_count, wf_scene;
     uint32_t* pinned_counts = nullptr;  // lagged queue lengths read by the launch loop
     std::vector<cudaEvent_t> count_events;
     // optional per-kernel timing of the last trace
@@ -92,6 +94,23 @@ struct tracer_ctx {
     cudaEvent_t prof_begin = nullptr, prof_end = nullptr;
     uint32_t last_rounds = 0, last_launches = 0;
     int last_kernel = 0;
+    // batch of scenes (tracer_upload_scenes / tracer_trace_batched)
+    SceneBuffers batch;                 // arena: every scene's arrays back to back
+    std::vector<DevScene> batch_scenes; // pointers into the arena, one per scene
+    std::vector<uint32_t> batch_depth, batch_nodes;
+    bool batch_emitters = false;
+    DevBuf<TraceArgs> batch_slots;
+    TraceArgs* pinned_slots = nullptr;
+    uint32_t pinned_slots_n = 0;
+    std::vector<size_t> batch_base;
+    std::vector<uint32_t> batch_w, batch_h;
+    DevBuf<uchar4> b_rgba8;
+    DevBuf<float4> b_rgba32f;
+    DevBuf<uint2> b_hit;
+    uint32_t b_mask = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<uint64_t> graph_key;
 };
 
 namespace {
@@ -178,6 +197,7 @@ void release_wavefront(tracer_ctx* c)
     c->wf_prim0.release();
     c->wf_q0.release();
     c->wf_q1.release();
+    c->wf_scene.release();
 }
 
 cudaError_t ensure_wavefront(tracer_ctx* c, size_t npx)
@@ -203,6 +223,47 @@ cudaEvent_t prof_event(tracer_ctx* c, size_t i)
         c->prof_events.push_back(ev);
     }
     return c->prof_events[i];
+}
+
+// Launches the wavefront: generate, then rounds of extend + shade until the
+// path queue is empty (read back a few rounds behind the launches) or
+// max_rounds is reached (no path needs more than spp * max_depth rounds).
+int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots, uint64_t max_rounds,
+                  uint32_t stack, uint32_t wavefront, cudaStream_t st)
+{
+    WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
+               c->wf_prim0.p, {c->wf_q0.p, c->wf_q1.p}, c->wf_count.p, c->wf_scene.p};
+    int per = wf_extend_blocks_per_sm(wc, stack);
+    if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "extend kernel cannot be resident (stack %u)", stack);
+    if (wavefront && (int)wavefront < per) per = (int)wavefront;
+    wc.extend_grid = (uint32_t)(per * c->sm_count);
+    const size_t sg = (nslots + 255) / 256;
+    wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
+    cudaError_t e = wf_launch_generate(a, ws, wc, st);
+    c->last_launches += 1;
+    for (uint64_t r = 0; r < max_rounds && e == cudaSuccess; ++r) {
+        const int qsel = (int)(r & 1);
+        if (c->profiling) cudaEventRecord(prof_event(c, 3 * r), st);
+        e = wf_launch_extend(a, ws, wc, qsel, st);
+        if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 1), st);
+        if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, qsel, st);
+        if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 2), st);
+        c->last_launches += 2;
+        c->last_rounds = (uint32_t)(r + 1);
+        const int slot = (int)(r % kCountSlots);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->pinned_counts + slot, c->wf_count.p + (qsel ^ 1), sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaEventRecord(c->count_events[slot], st);
+        if (e == cudaSuccess && r >= (uint64_t)kCountLag) {
+            const int old = (int)((r - kCountLag) % kCountSlots);
+            int w = wait_event(c, c->count_events[old]);
+            if (w != TRACER_OK) return w;
+            if (c->pinned_counts[old] == 0) break;
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
+    return TRACER_OK;
 }
 
 // Builds (or validates) one BVH; returns the leaf-order permutation.
@@ -292,6 +353,14 @@ void tracer_destroy(tracer_ctx* c)
     cudaSetDevice(c->device);
     if (c->pending && c->done) wait_event(c, c->done);
     c->scene.release();
+    c->batch.release();
+    c->batch_slots.release();
+    c->b_rgba8.release();
+    c->b_rgba32f.release();
+    c->b_hit.release();
+    if (c->pinned_slots) cudaFreeHost(c->pinned_slots);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
     c->rgba8.release();
     c->rgba32f.release();
     c->hit.release();
@@ -439,6 +508,8 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     uint32_t block = p->block ? p->block : 128;
     if (block % 32 != 0 || block < 32 || block > 256)
         return fail(c, TRACER_ERR_INVALID_ARG, "block %u must be a multiple of 32 in [32, 256]", block);
+    if (kernel == TRACER_KERNEL_WAVEFRONT && block != 64 && block != 128 && block != 256)
+        return fail(c, TRACER_ERR_INVALID_ARG, "wavefront block must be 64, 128 or 256");
     uint32_t need = c->scene.bvh ? (c->scene.depth > 1 ? c->scene.depth : 1) : 0;
     uint32_t stack = p->stack_depth ? p->stack_depth : need;
     if (c->scene.bvh && stack < need)
@@ -508,45 +579,17 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     } else {
         e = ensure_wavefront(c, npx);
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront state allocation");
-        WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
-                   c->wf_prim0.p, {c->wf_q0.p, c->wf_q1.p}, c->wf_count.p};
+        a.pixel_base = 0;
+        a.num_slots = (uint32_t)npx;
         WfConfig wc;
+        std::memset(&wc, 0, sizeof wc);
         wc.tie = p->tie_mode;
         wc.bvh = s.bvh ? 1 : 0;
         wc.stats = stats;
-        int per = wf_extend_blocks_per_sm(stack, wc.bvh, wc.tie, stats);
-        if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "extend kernel cannot be resident (stack %u)", stack);
-        if (p->wavefront && (int)p->wavefront < per) per = (int)p->wavefront;
-        wc.extend_grid = (uint32_t)(per * c->sm_count);
-        const size_t sg = (npx + 255) / 256;
-        wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
-        e = wf_launch_generate(a, ws, st);
-        c->last_launches = 1;
-        // Each round advances every live path by one bounce; no path needs
-        // more than spp * max_depth rounds.  The loop stops once a queue comes
-        // back empty, reading queue lengths a few rounds behind the launches.
-        const uint64_t max_rounds = (uint64_t)p->spp * p->max_depth + 1;
-        for (uint64_t r = 0; r < max_rounds && e == cudaSuccess; ++r) {
-            const int qsel = (int)(r & 1);
-            if (c->profiling) cudaEventRecord(prof_event(c, 3 * r), st);
-            e = wf_launch_extend(a, ws, wc, qsel, st);
-            if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 1), st);
-            if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, qsel, st);
-            if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 2), st);
-            c->last_launches += 2;
-            c->last_rounds = (uint32_t)(r + 1);
-            const int slot = (int)(r % kCountSlots);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(c->pinned_counts + slot, c->wf_count.p + (qsel ^ 1), sizeof(uint32_t),
-                                    cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaEventRecord(c->count_events[slot], st);
-            if (e == cudaSuccess && r >= (uint64_t)kCountLag) {
-                const int old = (int)((r - kCountLag) % kCountSlots);
-                int w = wait_event(c, c->count_events[old]);
-                if (w != TRACER_OK) return w;
-                if (c->pinned_counts[old] == 0) break;
-            }
-        }
+        wc.has_emitters = s.ne > 0;
+        wc.block = p->block ? p->block : 128;
+        r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, stack, p->wavefront, st);
+        if (r != TRACER_OK) return r;
     }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
     if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
@@ -738,18 +781,23 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     a.hit = nullptr;
     a.stats = reinterpret_cast<unsigned long long*>(base + kNaOffStats);
     a.status = reinterpret_cast<int*>(base + kNaOffStatus);
+    a.pixel_base = 0;
+    a.num_slots = p->width * p->height;
 
     WfState ws{reinterpret_cast<float4*>(base + kNaOffRayO), reinterpret_cast<float4*>(base + kNaOffRayD),
                reinterpret_cast<uint4*>(base + kNaOffHit), reinterpret_cast<float4*>(base + kNaOffAcc),
                reinterpret_cast<float4*>(base + kNaOffMask), reinterpret_cast<float4*>(base + kNaOffAccum),
                reinterpret_cast<uint32_t*>(base + kNaOffPrim0),
                {reinterpret_cast<uint32_t*>(base + kNaOffQ0), reinterpret_cast<uint32_t*>(base + kNaOffQ1)},
-               reinterpret_cast<uint32_t*>(base + kNaOffCount)};
+               reinterpret_cast<uint32_t*>(base + kNaOffCount), nullptr};
     WfConfig wc;
+    std::memset(&wc, 0, sizeof wc);
     wc.tie = p->tie_mode;
     wc.bvh = s.bvh ? 1 : 0;
     wc.stats = 0;
-    int per = wf_extend_blocks_per_sm(stack, wc.bvh, wc.tie, 0);
+    wc.has_emitters = s.ne > 0;
+    wc.block = 128;
+    int per = wf_extend_blocks_per_sm(wc, stack);
     if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "extend kernel cannot be resident (stack %u)", stack);
     if (p->wavefront && (int)p->wavefront < per) per = (int)p->wavefront;
     wc.extend_grid = (uint32_t)(per * c->sm_count);
@@ -760,7 +808,7 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     // The status word starts at zero; the generate kernel resets the queue
     // counters; statistics are not collected here.
     cudaError_t e = cudaMemsetAsync(a.status, 0, sizeof(int), st);
-    if (e == cudaSuccess) e = wf_launch_generate(a, ws, st);
+    if (e == cudaSuccess) e = wf_launch_generate(a, ws, wc, st);
     // Every round is launched (no queue length is read back to the host); a
     // round with an empty queue returns at once.
     const uint32_t rounds = p->spp * p->max_depth + 1;
@@ -769,5 +817,411 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
         if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, (int)(k & 1), st);
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "no-alloc trace launch");
+    return TRACER_OK;
+}
+
+// ------------------------------------------------------------------ batches
+namespace {
+
+// One scene packed for the device: triangles in leaf order as (v0, material)
+// (v1 - v0, id) (v2 - v0, 0), sphere centres/radii in leaf order, BVH nodes.
+struct PackedScene {
+    std::vector<float4> tri, geo;
+    std::vector<uint32_t> sid, emit;
+    std::vector<tracer_bvh_node> tnodes, snodes;
+    uint32_t depth = 0;
+    int status = TRACER_OK;
+};
+
+void pack_scene(const tracer_scene_desc& d, PackedScene& out)
+{
+    std::vector<uint32_t> tidx, sidx;
+    uint32_t td = 0, sd = 0;
+    if (d.num_triangles) {
+        if (d.tri_nodes) {
+            out.status = tracer_validate_bvh(TRACER_PRIM_TRIANGLE, d.triangles, d.num_triangles, d.tri_nodes,
+                                             d.num_tri_nodes, d.tri_prim_index, &td);
+            if (out.status != TRACER_OK) return;
+            out.tnodes.assign(d.tri_nodes, d.tri_nodes + d.num_tri_nodes);
+            tidx.assign(d.tri_prim_index, d.tri_prim_index + d.num_triangles);
+        } else {
+            out.tnodes.resize(2 * (size_t)d.num_triangles);
+            tidx.resize(d.num_triangles);
+            uint32_t nn = 0;
+            out.status = tracer_build_bvh(d.bvh, TRACER_PRIM_TRIANGLE, d.triangles, d.num_triangles, d.leaf_size,
+                                          d.sah_bins, out.tnodes.data(), &nn, tidx.data(), &td);
+            if (out.status != TRACER_OK) return;
+            out.tnodes.resize(nn);
+        }
+    }
+    if (d.num_spheres) {
+        if (d.sphere_nodes) {
+            out.status = tracer_validate_bvh(TRACER_PRIM_SPHERE, d.spheres, d.num_spheres, d.sphere_nodes,
+                                             d.num_sphere_nodes, d.sphere_prim_index, &sd);
+            if (out.status != TRACER_OK) return;
+            out.snodes.assign(d.sphere_nodes, d.sphere_nodes + d.num_sphere_nodes);
+            sidx.assign(d.sphere_prim_index, d.sphere_prim_index + d.num_spheres);
+        } else {
+            out.snodes.resize(2 * (size_t)d.num_spheres);
+            sidx.resize(d.num_spheres);
+            uint32_t nn = 0;
+            out.status = tracer_build_bvh(d.bvh, TRACER_PRIM_SPHERE, d.spheres, d.num_spheres, d.leaf_size,
+                                          d.sah_bins, out.snodes.data(), &nn, sidx.data(), &sd);
+            if (out.status != TRACER_OK) return;
+            out.snodes.resize(nn);
+        }
+    }
+    out.depth = td > sd ? td : sd;
+    out.tri.resize(3 * (size_t)d.num_triangles);
+    for (uint32_t k = 0; k < d.num_triangles; ++k) {
+        const uint32_t i = tidx[k];
+        const tracer_triangle& t = d.triangles[i];
+        float m, id;
+        std::memcpy(&m, &t.material, 4);
+        std::memcpy(&id, &i, 4);
+        out.tri[3 * k + 0] = make_float4(t.v0[0], t.v0[1], t.v0[2], m);
+        out.tri[3 * k + 1] = make_float4(t.v1[0] - t.v0[0], t.v1[1] - t.v0[1], t.v1[2] - t.v0[2], id);
+        out.tri[3 * k + 2] = make_float4(t.v2[0] - t.v0[0], t.v2[1] - t.v0[1], t.v2[2] - t.v0[2], 0.0f);
+    }
+    out.geo.resize(d.num_spheres);
+    out.sid.resize(d.num_spheres);
+    for (uint32_t k = 0; k < d.num_spheres; ++k) {
+        const uint32_t i = sidx[k];
+        const tracer_sphere& q = d.spheres[i];
+        out.geo[k] = make_float4(q.P[0], q.P[1], q.P[2], q.r);
+        out.sid[k] = i;
+    }
+    for (uint32_t i = 0; i < d.num_spheres; ++i) {
+        const float* em = d.spheres[i].mat.emissive;
+        if (!(em[0] == 0.0f && em[1] == 0.0f && em[2] == 0.0f)) out.emit.push_back(i);
+    }
+}
+
+int validate_desc(tracer_ctx* c, const tracer_scene_desc& d, uint32_t k)
+{
+    if ((d.num_triangles && !d.triangles) || (d.num_spheres && !d.spheres) || (d.num_planes && !d.planes) ||
+        (d.num_materials && !d.materials))
+        return fail(c, TRACER_ERR_INVALID_ARG, "scene %u: null array with a nonzero count", k);
+    if (d.bvh != TRACER_BVH_MEDIAN && d.bvh != TRACER_BVH_SAH)
+        return fail(c, TRACER_ERR_INVALID_ARG, "scene %u: batches need a BVH (median or SAH)", k);
+    if ((uint64_t)d.num_triangles + d.num_spheres + d.num_planes >= 0xFFFFFFFFull)
+        return fail(c, TRACER_ERR_INVALID_ARG, "scene %u: too many primitives", k);
+    for (uint32_t i = 0; i < d.num_triangles; ++i)
+        if (d.triangles[i].material >= d.num_materials)
+            return fail(c, TRACER_ERR_INVALID_ARG, "scene %u: triangle %u uses material %u of %u", k, i,
+                        d.triangles[i].material, d.num_materials);
+    return TRACER_OK;
+}
+
+}  // namespace
+
+extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* descs, uint32_t n)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!descs || n == 0) return fail(c, TRACER_ERR_INVALID_ARG, "empty batch");
+    for (uint32_t k = 0; k < n; ++k) {
+        int r = validate_desc(c, descs[k], k);
+        if (r != TRACER_OK) return r;
+    }
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    // BVH builds in parallel on host threads (each scene is independent)
+    std::vector<PackedScene> packed(n);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = std::min<unsigned>(hw, n);
+    std::vector<std::thread> pool;
+    std::atomic<uint32_t> next{0};
+    for (unsigned t = 0; t < nt; ++t)
+        pool.emplace_back([&]() {
+            for (uint32_t k = next++; k < n; k = next++) pack_scene(descs[k], packed[k]);
+        });
+    for (auto& th : pool) th.join();
+    for (uint32_t k = 0; k < n; ++k)
+        if (packed[k].status != TRACER_OK)
+            return fail(c, packed[k].status, "scene %u: BVH build or validation failed", k);
+
+    // one arena per array kind, scenes back to back
+    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes;
+    std::vector<uint32_t> sid, emit;
+    struct Off {
+        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit;
+    };
+    std::vector<Off> off(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const tracer_scene_desc& d = descs[k];
+        const PackedScene& p = packed[k];
+        off[k] = Off{tri.size(), mats.size(), geo.size(), rec.size(), planes.size(), tnodes.size(), snodes.size(),
+                     sid.size(), emit.size()};
+        tri.insert(tri.end(), p.tri.begin(), p.tri.end());
+        const float4* m = reinterpret_cast<const float4*>(d.materials);
+        mats.insert(mats.end(), m, m + 3 * (size_t)d.num_materials);
+        geo.insert(geo.end(), p.geo.begin(), p.geo.end());
+        const float4* sr = reinterpret_cast<const float4*>(d.spheres);
+        rec.insert(rec.end(), sr, sr + 4 * (size_t)d.num_spheres);
+        const float4* pl = reinterpret_cast<const float4*>(d.planes);
+        planes.insert(planes.end(), pl, pl + 4 * (size_t)d.num_planes);
+        const float4* tn = reinterpret_cast<const float4*>(p.tnodes.data());
+        tnodes.insert(tnodes.end(), tn, tn + 2 * p.tnodes.size());
+        const float4* sn = reinterpret_cast<const float4*>(p.snodes.data());
+        snodes.insert(snodes.end(), sn, sn + 2 * p.snodes.size());
+        sid.insert(sid.end(), p.sid.begin(), p.sid.end());
+        emit.insert(emit.end(), p.emit.begin(), p.emit.end());
+    }
+    SceneBuffers& b = c->batch;
+    b.release();
+    cudaError_t e = upload(b.tri, tri.data(), tri.size());
+    if (e == cudaSuccess) e = upload(b.mats, mats.data(), mats.size());
+    if (e == cudaSuccess) e = upload(b.sph_geo, geo.data(), geo.size());
+    if (e == cudaSuccess) e = upload(b.sph_rec, rec.data(), rec.size());
+    if (e == cudaSuccess) e = upload(b.planes, planes.data(), planes.size());
+    if (e == cudaSuccess) e = upload(b.tri_nodes, tnodes.data(), tnodes.size());
+    if (e == cudaSuccess) e = upload(b.sph_nodes, snodes.data(), snodes.size());
+    if (e == cudaSuccess) e = upload(b.sph_id, sid.data(), sid.size());
+    if (e == cudaSuccess) e = upload(b.emit, emit.data(), emit.size());
+    if (e != cudaSuccess) {
+        b.release();
+        return cuda_fail(c, e, "batch upload");
+    }
+    c->batch_scenes.assign(n, DevScene{});
+    c->batch_depth.assign(n, 0);
+    c->batch_nodes.assign(n, 0);
+    c->batch_emitters = false;
+    for (uint32_t k = 0; k < n; ++k) {
+        const tracer_scene_desc& d = descs[k];
+        const PackedScene& p = packed[k];
+        auto at = [](auto& buf, size_t o) { return buf.p ? buf.p + o : nullptr; };
+        c->batch_scenes[k] = DevScene{at(b.tri, off[k].tri), at(b.mats, off[k].mats), at(b.sph_geo, off[k].geo),
+                                      at(b.sph_id, off[k].sid), at(b.sph_rec, off[k].rec), at(b.planes, off[k].planes),
+                                      at(b.emit, off[k].emit), at(b.tri_nodes, off[k].tnodes),
+                                      at(b.sph_nodes, off[k].snodes), d.num_triangles, d.num_materials, d.num_spheres,
+                                      d.num_planes, (uint32_t)p.emit.size(), (uint32_t)p.tnodes.size(),
+                                      (uint32_t)p.snodes.size()};
+        c->batch_depth[k] = p.depth;
+        c->batch_nodes[k] = (uint32_t)std::max(p.tnodes.size(), p.snodes.size());
+        c->batch_emitters = c->batch_emitters || !p.emit.empty();
+    }
+    b.nt = (uint32_t)(tri.size() / 3);
+    b.bvh = true;
+    b.loaded = true;
+    c->graph_key.clear();
+    return TRACER_OK;
+}
+
+extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, const tracer_trace_params* params,
+                                    uint32_t n, int use_graph, void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!frames || !params) return fail(c, TRACER_ERR_INVALID_ARG, "null frames or params");
+    if (!c->batch.loaded) return fail(c, TRACER_ERR_NO_SCENE, "no batch uploaded");
+    if (n != c->batch_scenes.size())
+        return fail(c, TRACER_ERR_INVALID_ARG, "batch holds %zu scenes, %u given", c->batch_scenes.size(), n);
+    const tracer_trace_params& p0 = params[0];
+    const int kernel = p0.kernel == TRACER_KERNEL_AUTO ? TRACER_KERNEL_WAVEFRONT : p0.kernel;
+    if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p0.kernel);
+    const uint32_t block = p0.block ? p0.block : 128;
+    if (kernel == TRACER_KERNEL_WAVEFRONT && block != 64 && block != 128 && block != 256)
+        return fail(c, TRACER_ERR_INVALID_ARG, "wavefront block must be 64, 128 or 256");
+    if (kernel == TRACER_KERNEL_PLAIN && (block % 32 != 0 || block < 32 || block > 256))
+        return fail(c, TRACER_ERR_INVALID_ARG, "block %u must be a multiple of 32 in [32, 256]", block);
+    uint32_t need = 1, max_nodes = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+        need = std::max(need, c->batch_depth[k]);
+        max_nodes = std::max(max_nodes, c->batch_nodes[k]);
+    }
+    const uint32_t stack = p0.stack_depth ? p0.stack_depth : need;
+    if (stack < need) return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
+    if ((size_t)stack * 256 * 8 > 200 * 1024)
+        return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
+    const uint32_t mask = p0.aov_mask ? p0.aov_mask : (1u << TRACER_AOV_RGBA8);
+    const int stats = (p0.stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
+    std::vector<size_t> base(n);
+    size_t total = 0;
+    uint64_t max_rounds = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+        const tracer_trace_params& p = params[k];
+        if (p.width == 0 || p.height == 0 || p.width > 32768 || p.height > 32768)
+            return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "scene %u: image size %ux%u", k, p.width, p.height);
+        if (p.spp == 0 || p.max_depth == 0 || p.max_depth > 1024 || p.spp > 1u << 20)
+            return fail(c, TRACER_ERR_INVALID_ARG, "scene %u: spp / max_depth out of range", k);
+        if (p.tie_mode != TRACER_TIES_STRICT) return fail(c, TRACER_ERR_INVALID_ARG, "batches use strict ties");
+        base[k] = total;
+        total += (size_t)p.width * p.height;
+        max_rounds = std::max<uint64_t>(max_rounds, (uint64_t)p.spp * p.max_depth + 1);
+    }
+    if (total >= 0xFFFFFFFFull) return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "batch has too many pixels");
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaSuccess;
+    if (mask & (1u << TRACER_AOV_RGBA8)) e = dalloc(c->b_rgba8, total);
+    if (e == cudaSuccess && (mask & (1u << TRACER_AOV_RGBA32F))) e = dalloc(c->b_rgba32f, total);
+    if (e == cudaSuccess && (mask & (1u << TRACER_AOV_PRIMARY_HIT))) e = dalloc(c->b_hit, total);
+    if (e == cudaSuccess) e = dalloc(c->batch_slots, n);
+    if (e == cudaSuccess && c->pinned_slots_n < n) {
+        if (c->pinned_slots) cudaFreeHost(c->pinned_slots);
+        c->pinned_slots = nullptr;
+        c->pinned_slots_n = 0;
+        e = cudaMallocHost(&c->pinned_slots, sizeof(TraceArgs) * n);
+        if (e == cudaSuccess) c->pinned_slots_n = n;
+    }
+    if (e == cudaSuccess && kernel == TRACER_KERNEL_WAVEFRONT) {
+        e = ensure_wavefront(c, total);
+        if (e == cudaSuccess) e = dalloc(c->wf_scene, total);
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "batch allocation");
+    c->b_mask = mask | (stats ? (1u << TRACER_AOV_STATS) : 0u);
+    c->batch_base = base;
+    c->batch_w.resize(n);
+    c->batch_h.resize(n);
+
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    // per-scene arguments, written to pinned memory and copied to the table
+    // (stream-ordered after the previous trace that read it)
+    TraceArgs* slots = c->pinned_slots;
+    for (uint32_t k = 0; k < n; ++k) {
+        const tracer_trace_params& p = params[k];
+        const tracer_frame& f = frames[k];
+        TraceArgs& a = slots[k];
+        std::memset(&a, 0, sizeof a);
+        a.sc = c->batch_scenes[k];
+        a.fr.aspect = f.aspect_ratio;
+        a.fr.seed = f.seed;
+        a.fr.cpos = V3{f.camera.pos[0], f.camera.pos[1], f.camera.pos[2]};
+        a.fr.cdir = V3{f.camera.dir[0], f.camera.dir[1], f.camera.dir[2]};
+        a.fr.cright = V3{f.camera.right[0], f.camera.right[1], f.camera.right[2]};
+        a.fr.cup = V3{f.camera.up[0], f.camera.up[1], f.camera.up[2]};
+        a.width = p.width;
+        a.height = p.height;
+        a.spp = p.spp;
+        a.max_depth = p.max_depth;
+        a.rr_start = p.rr_start;
+        a.sky = V3{p.sky[0], p.sky[1], p.sky[2]};
+        a.sky_on = !(p.sky[0] == 0.0f && p.sky[1] == 0.0f && p.sky[2] == 0.0f);
+        a.stack_depth = stack;
+        a.trav_limit = 2 * c->batch_nodes[k] + 16;
+        a.rgba8 = (mask & (1u << TRACER_AOV_RGBA8)) ? c->b_rgba8.p + base[k] : nullptr;
+        a.rgba32f = (mask & (1u << TRACER_AOV_RGBA32F)) ? c->b_rgba32f.p + base[k] : nullptr;
+        a.hit = (mask & (1u << TRACER_AOV_PRIMARY_HIT)) ? c->b_hit.p + base[k] : nullptr;
+        a.stats = c->stats.p;
+        a.status = c->status.p;
+        a.pixel_base = (uint32_t)base[k];
+        a.num_slots = (uint32_t)total;
+        c->batch_w[k] = p.width;
+        c->batch_h[k] = p.height;
+    }
+    e = cudaMemcpyAsync(c->batch_slots.p, slots, sizeof(TraceArgs) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "batch set-up");
+    c->last_kernel = kernel;
+    c->last_rounds = 0;
+    c->last_launches = 0;
+    if (c->profiling) cudaEventRecord(c->prof_begin, st);
+
+    if (kernel == TRACER_KERNEL_PLAIN) {
+        LaunchConfig lc{block, stats, TRACER_TIES_STRICT, 1};
+        for (uint32_t k = 0; k < n && e == cudaSuccess; ++k) {
+            e = launch_plain(slots[k], lc, st);
+            c->last_launches++;
+        }
+    } else {
+        TraceArgs a = slots[0];
+        a.num_slots = (uint32_t)total;
+        a.stack_depth = stack;
+        a.trav_limit = 2 * max_nodes + 16;
+        WfConfig wc;
+        std::memset(&wc, 0, sizeof wc);
+        wc.tie = TRACER_TIES_STRICT;
+        wc.bvh = 1;
+        wc.stats = stats;
+        wc.multi = 1;
+        wc.has_emitters = c->batch_emitters;
+        wc.block = block;
+        wc.slots = c->batch_slots.p;
+        wc.nslots = n;
+        if (!use_graph) {
+            r = run_wavefront(c, a, wc, total, max_rounds, stack, p0.wavefront, st);
+            if (r != TRACER_OK) return r;
+        } else {
+            WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
+                       c->wf_prim0.p, {c->wf_q0.p, c->wf_q1.p}, c->wf_count.p, c->wf_scene.p};
+            int per = wf_extend_blocks_per_sm(wc, stack);
+            if (per <= 0) return fail(c, TRACER_ERR_INVALID_ARG, "extend kernel cannot be resident");
+            if (p0.wavefront && (int)p0.wavefront < per) per = (int)p0.wavefront;
+            wc.extend_grid = (uint32_t)(per * c->sm_count);
+            const size_t sg = (total + 255) / 256;
+            wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
+            // the graph bakes in sizes, launch shapes and buffer addresses
+            std::vector<uint64_t> key = {n, total, max_rounds, block, stack, (uint64_t)stats, wc.extend_grid,
+                                         (uint64_t)(uintptr_t)c->wf_ray_o.p, (uint64_t)(uintptr_t)c->batch_slots.p,
+                                         (uint64_t)(uintptr_t)c->b_rgba8.p, (uint64_t)(uintptr_t)c->b_rgba32f.p,
+                                         (uint64_t)(uintptr_t)c->b_hit.p, mask};
+            if (key != c->graph_key || !c->graph_exec) {
+                if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+                if (c->graph) cudaGraphDestroy(c->graph);
+                c->graph_exec = nullptr;
+                c->graph = nullptr;
+                c->graph_key.clear();
+                cudaStream_t cap;
+                e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+                if (e != cudaSuccess) return cuda_fail(c, e, "graph capture stream");
+                e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) e = wf_launch_generate(a, ws, wc, cap);
+                for (uint64_t k = 0; k < max_rounds && e == cudaSuccess; ++k) {
+                    e = wf_launch_extend(a, ws, wc, (int)(k & 1), cap);
+                    if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, (int)(k & 1), cap);
+                }
+                cudaGraph_t g = nullptr;
+                cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+                if (e == cudaSuccess) e = e2;
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+                cudaStreamDestroy(cap);
+                if (e != cudaSuccess) {
+                    if (g) cudaGraphDestroy(g);
+                    return cuda_fail(c, e, "graph capture");
+                }
+                c->graph = g;
+                c->graph_key = key;
+            }
+            e = cudaGraphLaunch(c->graph_exec, st);
+            c->last_rounds = (uint32_t)max_rounds;
+            c->last_launches = (uint32_t)(1 + 2 * max_rounds);
+        }
+    }
+    if (c->profiling) cudaEventRecord(c->prof_end, st);
+    if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "batched trace launch");
+    c->pending = true;
+    return TRACER_OK;
+}
+
+extern "C" int tracer_readback_scene(tracer_ctx* c, uint32_t scene, int aov, void* dst, size_t bytes)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!dst) return fail(c, TRACER_ERR_INVALID_ARG, "null destination");
+    if (scene >= c->batch_w.size()) return fail(c, TRACER_ERR_INVALID_ARG, "scene %u not in the last batch", scene);
+    cudaSetDevice(c->device);
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    const uint32_t bit = aov >= 0 && aov < 32 ? (1u << aov) : 0;
+    if (!bit || !(c->b_mask & bit))
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "AOV %d was not produced by the last batch", aov);
+    const size_t npx = (size_t)c->batch_w[scene] * c->batch_h[scene];
+    const size_t b = c->batch_base[scene];
+    const void* src;
+    size_t n;
+    switch (aov) {
+    case TRACER_AOV_RGBA8: src = c->b_rgba8.p + b; n = npx * 4; break;
+    case TRACER_AOV_RGBA32F: src = c->b_rgba32f.p + b; n = npx * 16; break;
+    case TRACER_AOV_PRIMARY_HIT: src = c->b_hit.p + b; n = npx * 8; break;
+    case TRACER_AOV_STATS: src = c->stats.p; n = sizeof(tracer_stats); break;
+    default: return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "unknown AOV %d", aov);
+    }
+    if (bytes != n) return fail(c, TRACER_ERR_INVALID_ARG, "AOV %d of scene %u holds %zu bytes, %zu requested", aov,
+                                scene, n, bytes);
+    cudaError_t e = cudaMemcpy(dst, src, n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "readback");
     return TRACER_OK;
 }

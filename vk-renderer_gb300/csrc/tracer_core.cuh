@@ -27,6 +27,10 @@ struct TraceArgs {
     uint2* hit;
     unsigned long long* stats;  // C_COUNT counters
     int* status;
+    // wavefront: first global path slot of this scene's pixels, and (in the
+    // launch's own arguments) the number of slots of the launch
+    uint32_t pixel_base;
+    uint32_t num_slots;
 };
 
 // Traversal stack of one thread in shared memory: entry i of thread t at

@@ -22,6 +22,11 @@
 //                runs across samples, :578-581); a finished pixel is resolved
 //                (:585-592).
 //
+// MULTI = true runs many scenes of different size and resolution in the same
+// queues (the batched form): every path slot belongs to one scene, whose
+// TraceArgs (scene pointers into one device arena, camera, image size,
+// parameters, output pointers) live in a device table.
+//
 // Per pixel the operations are exactly those of the plain kernel, in the same
 // order, so images and hits are identical to it and to the oracle.  Only the
 // order of node visits inside one ray's traversal differs (it depends on the
@@ -64,10 +69,15 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t*
     if (want) queue[base + __popc(m & ((1u << lane) - 1u))] = value;
 }
 
+// The TraceArgs a path belongs to: the launch's own (single scene) or its
+// scene's entry in the table (batched).
+#define SCENE_ARGS(MULTI, a, slots, sid) ((MULTI) ? (slots)[(sid)] : (a))
+
 // ---------------------------------------------------------------- generate --
-__global__ void __launch_bounds__(256) wf_generate(TraceArgs a, WfState s)
+template <bool MULTI>
+__global__ void __launch_bounds__(256) wf_generate(TraceArgs a, WfState s, const TraceArgs* slots, uint32_t nslots)
 {
-    const uint32_t n = a.width * a.height;
+    const uint32_t n = a.num_slots;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         s.count[0] = n;
@@ -75,10 +85,25 @@ __global__ void __launch_bounds__(256) wf_generate(TraceArgs a, WfState s)
         s.count[2] = 0;
     }
     if (i >= n) return;
-    const uint32_t x = i % a.width, y = i / a.width;
+    uint32_t sid = 0;
+    if (MULTI) {  // the scene whose slot range holds i: last pixel_base <= i
+        uint32_t lo = 0, hi = nslots;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (slots[mid].pixel_base <= i)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        sid = lo;
+        s.scene_of[i] = sid;
+    }
+    const TraceArgs& A = SCENE_ARGS(MULTI, a, slots, sid);
+    const uint32_t p = i - A.pixel_base;
+    const uint32_t x = p % A.width, y = p / A.width;
     Rng g;
-    seed_rng(a, x, y, g);
-    const Ray r = primary_ray(a, x, y);
+    seed_rng(A, x, y, g);
+    const Ray r = primary_ray(A, x, y);
     s.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, depth_tmax(0));
     s.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, 0.0f);
     s.acc[i] = make_float4(0.0f, 0.0f, 0.0f, g.salt);
@@ -89,33 +114,35 @@ __global__ void __launch_bounds__(256) wf_generate(TraceArgs a, WfState s)
 }
 
 // ------------------------------------------------------------------ extend --
-template <bool STATS>
+// Strict-tie acceptance without a separate tmax: the running best starts as
+// (t = tmax, prim = 0), so a candidate at exactly tmax fails the id test and
+// every candidate must satisfy t < tmax, as accept<TIE_STRICT> requires.
+__device__ __forceinline__ bool accept_strict(float t, uint32_t id, const Hit& h)
+{
+    return (t > EPSILON) && ((t < h.t) || (t == h.t && id < h.prim));
+}
+
 struct Lane {
     V3 o, d;
     BoxRay br;
-    float tmax;
     Hit h;
+    const float4* nodes;  // BVH of the current pass
+    const float4* prims;  // its primitives (triangles or sphere centres/radii)
     int cur, leaf, sp, pass;
-    uint32_t pid, steps;
+    uint32_t pid, scene, steps;
     bool has;
 };
 
-template <int TIE, bool STATS>
-__device__ __forceinline__ void write_hit(const WfState& s, uint32_t pid, const Hit& h)
-{
-    s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
-}
-
 // Planes after the BVHs (unbounded; scanned linearly, Tracer.comp:414-428).
-template <int TIE, bool STATS>
-__device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, Hit& h, float tmax, Counters& cnt)
+template <bool STATS>
+__device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, Hit& h, Counters& cnt)
 {
     for (uint32_t i = 0; i < sc.np; ++i) {
         if (STATS) cnt.c[C_PLANES]++;
         const float4 q = __ldg(sc.planes + 4 * (size_t)i + 3);
         const float tt = plane_intersect(ray, v3(q), q.w);
         const uint32_t id = sc.nt + sc.ns + i;
-        if (accept<TIE>(tt, id, h, tmax, true)) {
+        if (accept_strict(tt, id, h)) {
             h.t = tt;
             h.prim = id;
             h.kind = 3;
@@ -125,10 +152,11 @@ __device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, 
 }
 
 template <bool STATS>
-__device__ __forceinline__ void start_pass(const DevScene& sc, Lane<STATS>& L, Counters& cnt)
+__device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters& cnt)
 {
-    const float4* nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
-    const float4 lo = __ldg(nodes), hi = __ldg(nodes + 1);
+    L.nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
+    L.prims = L.pass == 0 ? sc.tri : sc.sph_geo;
+    const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
     if (STATS) cnt.c[C_NODES]++;
     float tn;
     L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? child_enc(lo, hi) : 0;
@@ -140,8 +168,7 @@ __device__ __forceinline__ void start_pass(const DevScene& sc, Lane<STATS>& L, C
     }
 }
 
-template <bool STATS>
-__device__ __forceinline__ int pop(Lane<STATS>& L, const Stack& stk)
+__device__ __forceinline__ int pop(Lane& L, const Stack& stk)
 {
     while (L.sp > 0) {
         --L.sp;
@@ -152,24 +179,22 @@ __device__ __forceinline__ int pop(Lane<STATS>& L, const Stack& stk)
     return 0;
 }
 
-template <int TIE, bool STATS>
-__global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, int qsel)
+template <int TIE, bool STATS, bool MULTI, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
+    wf_extend_bvh(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
     extern __shared__ int smem[];
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
-    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
-                    (int)blockDim.x, (int)a.stack_depth};
-    const DevScene& sc = a.sc;
+    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * BLOCK) + threadIdx.x,
+                    BLOCK, (int)a.stack_depth};
     const uint32_t total = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
-    const bool has_tri = sc.n_tri_nodes > 0 && sc.nt > 0;
-    const bool has_sph = sc.n_sph_nodes > 0 && sc.ns > 0;
     Counters cnt;
 #pragma unroll
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
-    Lane<STATS> L;
+    Lane L;
     L.has = false;
     bool exhausted = false;
     for (;;) {
@@ -186,23 +211,26 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                     exhausted = true;
                 } else {
                     L.pid = queue[qi];
+                    L.scene = MULTI ? s.scene_of[L.pid] : 0;
+                    const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
                     const float4 ro = s.ray_o[L.pid];
                     const float4 rd = s.ray_d[L.pid];
                     L.o = v3(ro);
                     L.d = v3(rd);
-                    L.tmax = ro.w;
                     L.h.t = ro.w;
-                    L.h.prim = NO_PRIM;
+                    L.h.prim = 0;  // see accept_strict
                     L.h.kind = 0;
                     L.h.slot = 0;
                     L.steps = 0;
                     if (STATS) cnt.c[C_CLOSEST]++;
                     L.has = true;
+                    const bool has_tri = sc.n_tri_nodes > 0 && sc.nt > 0;
+                    const bool has_sph = sc.n_sph_nodes > 0 && sc.ns > 0;
                     if (isnan3(L.d) || (!has_tri && !has_sph)) {
                         // no BVH work: NaN directions hit nothing; planes only
-                        if (!isnan3(L.d)) planes_pass<TIE, STATS>(sc, Ray{L.o, L.d}, L.h, L.tmax, cnt);
+                        if (!isnan3(L.d)) planes_pass<STATS>(sc, Ray{L.o, L.d}, L.h, cnt);
                         if (STATS && L.h.kind) cnt.c[C_HITS]++;
-                        write_hit<TIE, STATS>(s, L.pid, L.h);
+                        s.hit[L.pid] = make_uint4(__float_as_uint(L.h.t), L.h.prim, L.h.slot, (uint32_t)L.h.kind);
                         L.has = false;
                     } else {
                         L.br = make_boxray(Ray{L.o, L.d});
@@ -228,8 +256,7 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                     L.leaf = 0;
                     L.sp = 0;
                 } else {
-                    const float4* nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
-                    const float4* c = nodes + 2 * (size_t)L.cur;
+                    const float4* c = L.nodes + 2 * (size_t)L.cur;
                     const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
                     if (STATS) cnt.c[C_NODES] += 2;
                     float t0, t1;
@@ -237,7 +264,7 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                     const bool h1 = box_hit(L.br, lo1, hi1, L.h.t, t1);
                     const int e0 = child_enc(lo0, hi0), e1 = child_enc(lo1, hi1);
                     if (!h0 && !h1) {
-                        L.cur = pop<STATS>(L, stk);
+                        L.cur = pop(L, stk);
                     } else {
                         const bool swap = h1 && (!h0 || t1 < t0);
                         L.cur = swap ? e1 : e0;
@@ -253,7 +280,7 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                     }
                     if (L.cur < 0 && L.leaf == 0) {
                         L.leaf = L.cur;
-                        L.cur = pop<STATS>(L, stk);
+                        L.cur = pop(L, stk);
                     }
                 }
             }
@@ -269,11 +296,11 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                 if (L.pass == 0) {
                     for (int k = 0; k < count; ++k) {
                         if (STATS) cnt.c[C_TRIS]++;
-                        const float4* t = sc.tri + 3 * (size_t)(first + k);
+                        const float4* t = L.prims + 3 * (size_t)(first + k);
                         const float4 ta = __ldg(t), tb = __ldg(t + 1), tc = __ldg(t + 2);
                         const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
                         const uint32_t id = __float_as_uint(tb.w);
-                        if (accept<TIE>(tt, id, L.h, L.tmax, false)) {
+                        if (accept_strict(tt, id, L.h)) {
                             L.h.t = tt;
                             L.h.prim = id;
                             L.h.kind = 1;
@@ -281,12 +308,13 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                         }
                     }
                 } else {
+                    const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
                     for (int k = 0; k < count; ++k) {
                         if (STATS) cnt.c[C_SPHERES]++;
-                        const float4 gg = __ldg(sc.sph_geo + first + k);
+                        const float4 gg = __ldg(L.prims + first + k);
                         const float tt = sphere_intersect(ray, v3(gg), gg.w);
                         const uint32_t id = sc.nt + __ldg(sc.sph_id + first + k);
-                        if (accept<TIE>(tt, id, L.h, L.tmax, false)) {
+                        if (accept_strict(tt, id, L.h)) {
                             L.h.t = tt;
                             L.h.prim = id;
                             L.h.kind = 2;
@@ -296,7 +324,7 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
                 }
                 if (L.cur < 0) {
                     L.leaf = L.cur;
-                    L.cur = pop<STATS>(L, stk);
+                    L.cur = pop(L, stk);
                 } else {
                     L.leaf = 0;
                 }
@@ -304,13 +332,14 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
         }
         // 4) finished passes: next primitive kind, or planes and the result
         if (L.has && L.cur == 0 && L.leaf == 0) {
-            if (L.pass == 0 && has_sph) {
+            const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
+            if (L.pass == 0 && sc.n_sph_nodes > 0 && sc.ns > 0) {
                 L.pass = 1;
                 start_pass<STATS>(sc, L, cnt);
             } else {
-                planes_pass<TIE, STATS>(sc, Ray{L.o, L.d}, L.h, L.tmax, cnt);
+                planes_pass<STATS>(sc, Ray{L.o, L.d}, L.h, cnt);
                 if (STATS && L.h.kind) cnt.c[C_HITS]++;
-                write_hit<TIE, STATS>(s, L.pid, L.h);
+                s.hit[L.pid] = make_uint4(__float_as_uint(L.h.t), L.h.prim, L.h.slot, (uint32_t)L.h.kind);
                 L.has = false;
             }
         }
@@ -319,7 +348,7 @@ __global__ void __launch_bounds__(128, 8) wf_extend_bvh(TraceArgs a, WfState s, 
 }
 
 // Linear-scan scenes (the reference's own trace_ray, reference or strict ties):
-// persistent lanes with the same warp-aggregated fetch.
+// persistent lanes with a per-warp fetch.  Single scene only.
 template <int TIE, bool STATS>
 __global__ void __launch_bounds__(128) wf_extend_linear(TraceArgs a, WfState s, int qsel)
 {
@@ -352,21 +381,19 @@ __global__ void __launch_bounds__(128) wf_extend_linear(TraceArgs a, WfState s, 
 }
 
 // ------------------------------------------------------------------- shade --
-template <int TIE, bool BVH, bool STATS>
-__global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel)
+template <int TIE, bool BVH, bool STATS, bool MULTI>
+__global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
     extern __shared__ int smem[];
     const uint32_t n = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
+    uint32_t* next = qsel ? s.queue[0] : s.queue[1];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // extend's fetch cursor for the next round
     Counters cnt;
 #pragma unroll
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
-    Tracer<TIE, BVH, STATS> tr{a.sc,
-                               Stack{smem + threadIdx.x,
-                                     reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
-                                     (int)blockDim.x, (int)a.stack_depth},
-                               cnt, a.status, a.trav_limit};
+    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
+                    (int)blockDim.x, (int)a.stack_depth};
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t qi = base + threadIdx.x;
@@ -375,17 +402,20 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
         uint32_t pid = 0;
         if (active) {
             pid = queue[qi];
-            const uint32_t x = pid % a.width, y = pid / a.width;
+            const TraceArgs& A = SCENE_ARGS(MULTI, a, slots, MULTI ? s.scene_of[pid] : 0);
+            Tracer<TIE, BVH, STATS> tr{A.sc, stk, cnt, a.status, A.trav_limit};
+            const uint32_t p = pid - A.pixel_base;
+            const uint32_t x = p % A.width, y = p / A.width;
             const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
             const uint4 hr = s.hit[pid];
-            float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
+            const float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
             uint32_t prim0 = s.prim0[pid];
             const uint32_t sd = __float_as_uint(accum4.w);
             uint32_t sample = sd >> 16, depth = sd & 0xFFFFu;
             Rng g;
             g.salt = acc4.w;
-            g.cx = (float)x / (float)a.width;
-            g.cy = (float)y / (float)a.height;
+            g.cx = (float)x / (float)A.width;
+            g.cy = (float)y / (float)A.height;
             V3 acc = vclamp01(v3(acc4));
             V3 mask = v3(mask4);
             Hit h;
@@ -400,22 +430,22 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
                 t0 = found ? h.t : -1.0f;
             }
             Ray ray{v3(ro), v3(rd)};
-            const bool cont = shade_bounce(tr, a, depth, found, h, ray, acc, mask, g);
+            const bool cont = shade_bounce(tr, A, depth, found, h, ray, acc, mask, g);
             depth++;
             V3 accum = v3(accum4);
-            if (cont && depth < a.max_depth) {
+            if (cont && depth < A.max_depth) {
                 again = true;
             } else {
                 accum = accum + acc;
                 sample++;
                 depth = 0;
-                if (sample < a.spp) {
-                    ray = primary_ray(a, x, y);
+                if (sample < A.spp) {
+                    ray = primary_ray(A, x, y);
                     acc = splat(0.0f);
                     mask = splat(1.0f);
                     again = true;
                 } else {
-                    resolve_pixel(a, x, y, accum, g, prim0, t0);
+                    resolve_pixel(A, x, y, accum, g, prim0, t0);
                 }
             }
             if (again) {
@@ -427,48 +457,72 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
                 s.prim0[pid] = prim0;
             }
         }
-        warp_append(again, pid, qsel ? s.queue[0] : s.queue[1], &s.count[qsel ^ 1]);
+        warp_append(again, pid, next, &s.count[qsel ^ 1]);
     }
     if (STATS) flush_counters(a, cnt);
 }
 
 // ---------------------------------------------------------------- dispatch --
-template <int TIE, bool BVH, bool STATS>
+template <class K>
+static void smem_attr(K k, size_t smem)
+{
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <int TIE, bool STATS, bool MULTI, int BLOCK>
+static cudaError_t extend_bvh_b(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    auto k = wf_extend_bvh<TIE, STATS, MULTI, BLOCK>;
+    const size_t smem = (size_t)a.stack_depth * BLOCK * 8;
+    smem_attr(k, smem);
+    k<<<c.extend_grid, BLOCK, smem, st>>>(a, s, qsel, c.slots);
+    return cudaGetLastError();
+}
+
+template <int TIE, bool BVH, bool STATS, bool MULTI>
 static cudaError_t extend_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
     if (BVH) {
-        auto k = wf_extend_bvh<TIE, STATS>;
-        const size_t smem = (size_t)a.stack_depth * 128 * 8;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<c.extend_grid, 128, smem, st>>>(a, s, qsel);
-    } else {
-        wf_extend_linear<TIE, STATS><<<c.extend_grid, 128, 0, st>>>(a, s, qsel);
+        if (c.block == 64) return extend_bvh_b<TIE, STATS, MULTI, 64>(a, s, c, qsel, st);
+        if (c.block == 256) return extend_bvh_b<TIE, STATS, MULTI, 256>(a, s, c, qsel, st);
+        return extend_bvh_b<TIE, STATS, MULTI, 128>(a, s, c, qsel, st);
     }
+    wf_extend_linear<TIE, STATS><<<c.extend_grid, 128, 0, st>>>(a, s, qsel);
     return cudaGetLastError();
 }
 
-template <int TIE, bool BVH, bool STATS>
+template <int TIE, bool BVH, bool STATS, bool MULTI>
 static cudaError_t shade_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
-    auto k = wf_shade<TIE, BVH, STATS>;
-    const size_t smem = (BVH && a.sc.ne) ? (size_t)a.stack_depth * 256 * 8 : 0;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<c.shade_grid, 256, smem, st>>>(a, s, qsel);
+    auto k = wf_shade<TIE, BVH, STATS, MULTI>;
+    const size_t smem = (BVH && c.has_emitters) ? (size_t)a.stack_depth * 256 * 8 : 0;
+    smem_attr(k, smem);
+    k<<<c.shade_grid, 256, smem, st>>>(a, s, qsel, c.slots);
     return cudaGetLastError();
 }
 
-#define WF_DISPATCH(fn)                                                                                   \
-    if (c.tie == TIE_REFERENCE)                                                                           \
-        return c.stats ? fn<TIE_REFERENCE, false, true>(a, s, c, qsel, st)                                \
-                       : fn<TIE_REFERENCE, false, false>(a, s, c, qsel, st);                              \
-    if (c.bvh)                                                                                            \
-        return c.stats ? fn<TIE_STRICT, true, true>(a, s, c, qsel, st) : fn<TIE_STRICT, true, false>(a, s, c, qsel, st); \
-    return c.stats ? fn<TIE_STRICT, false, true>(a, s, c, qsel, st) : fn<TIE_STRICT, false, false>(a, s, c, qsel, st);
+// Template selection: ties, BVH (strict only), statistics, multi-scene (BVH only).
+#define WF_DISPATCH(fn)                                                                                    \
+    if (c.multi) {                                                                                         \
+        return c.stats ? fn<TIE_STRICT, true, true, true>(a, s, c, qsel, st)                              \
+                       : fn<TIE_STRICT, true, false, true>(a, s, c, qsel, st);                            \
+    }                                                                                                      \
+    if (c.tie == TIE_REFERENCE)                                                                            \
+        return c.stats ? fn<TIE_REFERENCE, false, true, false>(a, s, c, qsel, st)                         \
+                       : fn<TIE_REFERENCE, false, false, false>(a, s, c, qsel, st);                       \
+    if (c.bvh)                                                                                             \
+        return c.stats ? fn<TIE_STRICT, true, true, false>(a, s, c, qsel, st)                             \
+                       : fn<TIE_STRICT, true, false, false>(a, s, c, qsel, st);                           \
+    return c.stats ? fn<TIE_STRICT, false, true, false>(a, s, c, qsel, st)                                \
+                   : fn<TIE_STRICT, false, false, false>(a, s, c, qsel, st);
 
-cudaError_t wf_launch_generate(const TraceArgs& a, const WfState& s, cudaStream_t st)
+cudaError_t wf_launch_generate(const TraceArgs& a, const WfState& s, const WfConfig& c, cudaStream_t st)
 {
-    const uint32_t n = a.width * a.height;
-    wf_generate<<<(n + 255) / 256, 256, 0, st>>>(a, s);
+    const uint32_t n = a.num_slots;
+    if (c.multi)
+        wf_generate<true><<<(n + 255) / 256, 256, 0, st>>>(a, s, c.slots, c.nslots);
+    else
+        wf_generate<false><<<(n + 255) / 256, 256, 0, st>>>(a, s, nullptr, 0);
     return cudaGetLastError();
 }
 
@@ -482,22 +536,42 @@ cudaError_t wf_launch_shade(const TraceArgs& a, const WfState& s, const WfConfig
     WF_DISPATCH(shade_t)
 }
 
-int wf_extend_blocks_per_sm(uint32_t stack_depth, int bvh, int tie, int stats)
+template <int TIE, bool STATS, bool MULTI>
+static int occ_bvh(uint32_t block, size_t stack_depth)
 {
     int n = 0;
-    const size_t smem = (size_t)stack_depth * 128 * 8;
     cudaError_t e;
-    if (bvh) {
-        auto k = stats ? wf_extend_bvh<TIE_STRICT, true> : wf_extend_bvh<TIE_STRICT, false>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, smem);
-    } else if (tie == TIE_REFERENCE) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, stats ? wf_extend_linear<TIE_REFERENCE, true> : wf_extend_linear<TIE_REFERENCE, false>, 128, 0);
+    const size_t smem = stack_depth * block * 8;
+    if (block == 64) {
+        auto k = wf_extend_bvh<TIE, STATS, MULTI, 64>;
+        smem_attr(k, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 64, smem);
+    } else if (block == 256) {
+        auto k = wf_extend_bvh<TIE, STATS, MULTI, 256>;
+        smem_attr(k, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, smem);
     } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, stats ? wf_extend_linear<TIE_STRICT, true> : wf_extend_linear<TIE_STRICT, false>, 128, 0);
+        auto k = wf_extend_bvh<TIE, STATS, MULTI, 128>;
+        smem_attr(k, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, smem);
     }
+    return e == cudaSuccess ? n : 0;
+}
+
+int wf_extend_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
+{
+    if (c.multi) return c.stats ? occ_bvh<TIE_STRICT, true, true>(c.block, stack_depth)
+                                : occ_bvh<TIE_STRICT, false, true>(c.block, stack_depth);
+    if (c.bvh) return c.stats ? occ_bvh<TIE_STRICT, true, false>(c.block, stack_depth)
+                              : occ_bvh<TIE_STRICT, false, false>(c.block, stack_depth);
+    int n = 0;
+    cudaError_t e;
+    if (c.tie == TIE_REFERENCE)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, c.stats ? wf_extend_linear<TIE_REFERENCE, true> : wf_extend_linear<TIE_REFERENCE, false>, 128, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &n, c.stats ? wf_extend_linear<TIE_STRICT, true> : wf_extend_linear<TIE_STRICT, false>, 128, 0);
     return e == cudaSuccess ? n : 0;
 }
 

@@ -38,7 +38,8 @@ EXPORTED_SYMBOLS = [
     "tracer_create", "tracer_destroy", "tracer_last_error", "tracer_status_string", "tracer_set_timeout",
     "tracer_upload_scene", "tracer_set_materials", "tracer_trace", "tracer_readback", "tracer_synchronize",
     "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh", "tracer_set_profiling",
-    "tracer_last_timings", "tracer_trace_noalloc",
+    "tracer_last_timings", "tracer_trace_noalloc", "tracer_upload_scenes", "tracer_trace_batched",
+    "tracer_readback_scene",
 ]
 NOALLOC_MAX_PIXELS = 16384
 NOALLOC_MAX_ROUNDS = 8192
@@ -110,6 +111,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_set_profiling.argtypes = [vp, i32]
     lib.tracer_last_timings.argtypes = [vp, ctypes.POINTER(Timings)]
     lib.tracer_trace_noalloc.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp, vp, vp]
+    lib.tracer_upload_scenes.argtypes = [vp, ctypes.POINTER(SceneDesc), u32]
+    lib.tracer_trace_batched.argtypes = [vp, vp, ctypes.POINTER(TraceParams), u32, i32, vp]
+    lib.tracer_readback_scene.argtypes = [vp, u32, i32, vp, sz]
     if path is None:
         _lib = lib
     return lib
@@ -180,9 +184,10 @@ class Tracer:
     def set_timeout(self, ms: int):
         self._check(self.lib.tracer_set_timeout(self.h, ms))
 
-    def upload_scene(self, sc: S.Scene, tri_bvh=None, sphere_bvh=None):
+    @staticmethod
+    def _fill_desc(d: SceneDesc, sc: S.Scene, tri_bvh=None, sphere_bvh=None) -> list:
+        """Fills a tracer_scene_desc; returns the arrays it points into (keep alive)."""
         arrs = [np.ascontiguousarray(a) for a in (sc.triangles, sc.materials, sc.spheres, sc.planes)]
-        d = SceneDesc()
         d.triangles, d.num_triangles = _ptr(arrs[0]), len(arrs[0])
         d.materials, d.num_materials = _ptr(arrs[1]), len(arrs[1])
         d.spheres, d.num_spheres = _ptr(arrs[2]), len(arrs[2])
@@ -197,7 +202,42 @@ class Tracer:
             nodes, idx = np.ascontiguousarray(sphere_bvh[0]), np.ascontiguousarray(sphere_bvh[1], np.uint32)
             d.sphere_nodes, d.num_sphere_nodes, d.sphere_prim_index = _ptr(nodes), len(nodes), _ptr(idx)
             keep += [nodes, idx]
+        return keep
+
+    def upload_scene(self, sc: S.Scene, tri_bvh=None, sphere_bvh=None):
+        d = SceneDesc()
+        keep = self._fill_desc(d, sc, tri_bvh, sphere_bvh)
         self._check(self.lib.tracer_upload_scene(self.h, ctypes.byref(d)))
+        del keep
+
+    def upload_scenes(self, scenes: list):
+        """tracer_upload_scenes: a batch packed into one device arena."""
+        descs = (SceneDesc * len(scenes))()
+        keep = [self._fill_desc(descs[i], sc) for i, sc in enumerate(scenes)]
+        self._check(self.lib.tracer_upload_scenes(self.h, descs, len(scenes)))
+        self.batch_sizes = [None] * len(scenes)
+        del keep
+
+    def trace_batched(self, frames: list, params: list, use_graph: bool = True, stream: int | None = None):
+        n = len(frames)
+        fr = np.zeros(n, S.FRAME)
+        for i, f in enumerate(frames):
+            fr[i] = np.asarray(f, S.FRAME).reshape(())
+        prm = (TraceParams * n)(*params)
+        self._check(self.lib.tracer_trace_batched(self.h, fr.ctypes.data_as(ctypes.c_void_p), prm, n,
+                                                  1 if use_graph else 0,
+                                                  ctypes.c_void_p(stream) if stream else None))
+        self.batch_sizes = [(p.width, p.height) for p in params]
+
+    def readback_scene(self, scene: int, aov: int, out: np.ndarray | None = None) -> np.ndarray:
+        w, h = self.batch_sizes[scene]
+        shape, dt = {AOV_RGBA8: ((h, w, 4), np.uint8), AOV_RGBA32F: ((h, w, 4), np.float32),
+                     AOV_PRIMARY_HIT: ((h, w, 2), np.uint32), AOV_STATS: ((len(STATS_FIELDS),), np.uint64)}[aov]
+        if out is None:
+            out = np.empty(shape, dt)
+        self._check(self.lib.tracer_readback_scene(self.h, scene, aov, out.ctypes.data_as(ctypes.c_void_p),
+                                                   out.nbytes))
+        return out
 
     def set_materials(self, mats: np.ndarray):
         mats = np.ascontiguousarray(mats, S.MATERIAL)

@@ -1,0 +1,92 @@
+"""Autotuner for the wavefront launch shape.
+
+Sweeps the extend kernel's block size, the traversal stack depth and the
+"wavefront size" (resident extend CTAs per SM, i.e. how many rays are in
+flight at once), timing each candidate on the device with CUDA events
+(tracer_last_timings), and returns the fastest.  Candidates the library
+refuses (a stack shallower than the BVH, a shape that cannot be resident)
+are recorded as skipped.  Results are deterministic given the timings.
+"""
+from __future__ import annotations
+
+import itertools
+import time
+
+from . import abi
+
+
+def _set(params, block, stack, wave):
+    for p in params:
+        p.block, p.stack_depth, p.wavefront = block, stack, wave
+
+
+def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stacks=(16, 32, 64),
+                     wavefronts=(0, 6, 4), reps: int = 1, use_graph: bool = True, budget_s: float = 60.0):
+    """Returns (best, table): best = dict(block, stack_depth, wavefront, ms);
+    table = one dict per candidate (ms or skipped reason)."""
+    table = []
+    best = None
+    t_start = time.perf_counter()
+    saved = [(p.block, p.stack_depth, p.wavefront) for p in params]
+    tr.set_profiling(True)
+    try:
+        for block, stack, wave in itertools.product(blocks, stacks, wavefronts):
+            if time.perf_counter() - t_start > budget_s:
+                table.append({"block": block, "stack_depth": stack, "wavefront": wave, "skipped": "time budget"})
+                continue
+            _set(params, block, stack, wave)
+            try:
+                tr.trace_batched(frames, params, use_graph=use_graph)  # first run: graph capture, caches warm
+                tr.synchronize()
+                times = []
+                for _ in range(reps):
+                    tr.trace_batched(frames, params, use_graph=use_graph)
+                    times.append(tr.timings()["total_ms"])
+                ms = sorted(times)[len(times) // 2]
+            except abi.TracerError as e:
+                table.append({"block": block, "stack_depth": stack, "wavefront": wave, "skipped": str(e)})
+                continue
+            row = {"block": block, "stack_depth": stack, "wavefront": wave, "ms": ms}
+            table.append(row)
+            if best is None or ms < best["ms"]:
+                best = dict(row)
+    finally:
+        tr.set_profiling(False)
+        for p, (b, s, w) in zip(params, saved):
+            p.block, p.stack_depth, p.wavefront = b, s, w
+    return best, table
+
+
+def autotune_single(tr: abi.Tracer, frame, params, blocks=(64, 128, 256), stacks=(0,), wavefronts=(0, 6, 4),
+                    reps: int = 1, budget_s: float = 60.0):
+    """The same sweep for one scene (tracer_trace, wavefront kernel)."""
+    table = []
+    best = None
+    t_start = time.perf_counter()
+    saved = (params.block, params.stack_depth, params.wavefront)
+    tr.set_profiling(True)
+    try:
+        for block, stack, wave in itertools.product(blocks, stacks, wavefronts):
+            if time.perf_counter() - t_start > budget_s:
+                table.append({"block": block, "stack_depth": stack, "wavefront": wave, "skipped": "time budget"})
+                continue
+            params.block, params.stack_depth, params.wavefront = block, stack, wave
+            try:
+                tr.trace(frame, params)
+                tr.synchronize()
+                times = []
+                for _ in range(reps):
+                    tr.trace(frame, params)
+                    times.append(tr.timings()["total_ms"])
+                ms = sorted(times)[len(times) // 2]
+            except abi.TracerError as e:
+                table.append({"block": block, "stack_depth": stack, "wavefront": wave, "skipped": str(e)})
+                continue
+            row = {"block": block, "stack_depth": stack, "wavefront": wave, "ms": ms}
+            table.append(row)
+            if best is None or ms < best["ms"]:
+                best = dict(row)
+    finally:
+        tr.set_profiling(False)
+        params.block, params.stack_depth, params.wavefront = saved
+    return best, table
