@@ -94,6 +94,29 @@ def test_graph_replay_follows_new_frames(gpu_tracer):
     assert np.array_equal(_bits(a), _bits(single))
 
 
+def test_timings_after_graph_and_autotune(gpu_tracer):
+    """Per-kernel timings after a graph replay (no per-round events exist) and
+    the autotuner's sweep over launch shapes."""
+    from vktrace import tune
+    tr = gpu_tracer
+    scenes, frames, params = _batch()
+    tr.upload_scenes(scenes)
+    tr.set_profiling(True)
+    try:
+        tr.trace_batched(frames, params, use_graph=True)
+        t = tr.timings()
+        assert t["total_ms"] > 0 and t["extend_ms"] == 0 and t["rounds"] > 0
+        tr.trace_batched(frames, params, use_graph=False)
+        t = tr.timings()
+        assert t["extend_ms"] > 0 and t["shade_ms"] > 0
+    finally:
+        tr.set_profiling(False)
+    best, table = tune.autotune_batched(tr, frames, params, blocks=(64, 128), stacks=(4, 32), wavefronts=(0, 2))
+    assert best is not None and best["ms"] > 0
+    assert any("skipped" in r for r in table)  # stack 4 is below the BVH depth
+    assert len(table) == 8
+
+
 def test_batched_argument_errors(gpu_tracer):
     tr = gpu_tracer
     scenes, frames, params = _batch()

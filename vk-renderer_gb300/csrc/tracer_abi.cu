@@ -93,6 +93,7 @@ struct tracer_ctx {
     std::vector<cudaEvent_t> prof_events;  // 3 per round: before extend, after extend, after shade
     cudaEvent_t prof_begin = nullptr, prof_end = nullptr;
     uint32_t last_rounds = 0, last_launches = 0;
+    uint32_t last_prof_rounds = 0;  // rounds of the last trace with per-kernel events recorded
     int last_kernel = 0;
     // batch of scenes (tracer_upload_scenes / tracer_trace_batched)
     SceneBuffers batch;                 // arena: every scene's arrays back to back
@@ -250,6 +251,7 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
         if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 2), st);
         c->last_launches += 2;
         c->last_rounds = (uint32_t)(r + 1);
+        if (c->profiling && c->prof_events.size() >= 3 * (r + 1)) c->last_prof_rounds = (uint32_t)(r + 1);
         const int slot = (int)(r % kCountSlots);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(c->pinned_counts + slot, c->wf_count.p + (qsel ^ 1), sizeof(uint32_t),
@@ -569,6 +571,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     if (e != cudaSuccess) return cuda_fail(c, e, "trace set-up");
     c->last_kernel = kernel;
     c->last_rounds = 0;
+    c->last_prof_rounds = 0;
     c->last_launches = 0;
     if (c->profiling) cudaEventRecord(c->prof_begin, st);
 
@@ -617,7 +620,7 @@ int tracer_last_timings(tracer_ctx* c, tracer_timings* out)
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, c->prof_begin, c->prof_end) == cudaSuccess) out->total_ms = ms;
     if (c->last_kernel == TRACER_KERNEL_WAVEFRONT) {
-        for (uint32_t i = 0; i < c->last_rounds; ++i) {
+        for (uint32_t i = 0; i < c->last_prof_rounds && 3 * (size_t)i + 2 < c->prof_events.size(); ++i) {
             if (cudaEventElapsedTime(&ms, c->prof_events[3 * i], c->prof_events[3 * i + 1]) == cudaSuccess)
                 out->extend_ms += ms;
             if (cudaEventElapsedTime(&ms, c->prof_events[3 * i + 1], c->prof_events[3 * i + 2]) == cudaSuccess)
@@ -1117,6 +1120,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
     if (e != cudaSuccess) return cuda_fail(c, e, "batch set-up");
     c->last_kernel = kernel;
     c->last_rounds = 0;
+    c->last_prof_rounds = 0;
     c->last_launches = 0;
     if (c->profiling) cudaEventRecord(c->prof_begin, st);
 
