@@ -181,6 +181,7 @@ typedef struct tracer_scene_desc {
 #define TRACER_AOV_RGBA32F 1     /* w*h*4 f32: the colour before UNORM8 conversion */
 #define TRACER_AOV_PRIMARY_HIT 2 /* w*h*(u32 prim id, f32 t) of the first ray of each pixel */
 #define TRACER_AOV_STATS 3       /* one tracer_stats */
+#define TRACER_AOV_LINEAR 4      /* w*h*4 f32: mean radiance accum / spp before tone mapping, alpha 1 */
 
 /* Primitive ids in PRIMARY_HIT: triangles 0..nt-1, spheres nt..nt+ns-1,
  * planes after; 0xFFFFFFFF (and t = -1) on a miss. */
@@ -243,6 +244,22 @@ int tracer_synchronize(tracer_ctx* ctx);
 /* Device address and size of an AOV of the last trace (zero-copy interop;
  * valid until the next trace with a different image size). */
 int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* bytes);
+
+/* ------------------------------------------------------------ adjoint
+ * Gradients of an image loss L with respect to the material table's albedo
+ * and emission and to the camera position (no counterpart in the reference).
+ * dL_dimage: w*h*4 floats, dL/dI for the RGBA32F image of the same frame and
+ * params (alpha ignored).  linear_image: the LINEAR AOV of the forward trace
+ * of that frame (w*h*4 floats), or NULL to recompute it.  Outputs (any may be
+ * NULL): d_albedo and d_emission num_materials*3 floats, d_campos 3 floats.
+ * Each pointer may be host or device memory; with host outputs the call
+ * waits (bounded) for the result, with device outputs it is asynchronous on
+ * cuda_stream.  Path replay: every sample is traced twice more (no path
+ * vertices are stored); the Russian-roulette normalisation is treated as a
+ * constant.  Materials of spheres and planes (stored inline) get no gradient. */
+int tracer_trace_adjoint(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
+                         const float* dL_dimage, const float* linear_image, float* d_albedo, float* d_emission,
+                         float* d_campos, void* cuda_stream);
 
 /* ------------------------------------------------------------ batches
  * Many independent scenes of uneven size and resolution traced together (no

@@ -41,6 +41,8 @@ typedef struct oracle_stats {
 
 int oracle_render(const oracle_scene* scene, const float* frame96, const oracle_params* params, float* rgba32f,
                   uint8_t* rgba8, uint32_t* hit_id, float* hit_t, oracle_stats* stats);
+/* FP64 evaluation (the RNG stays float).  accum: 4 doubles per pixel = the
+ * mean radiance accum / spp (3) and the pixel's dither rand() / 64. */
 int oracle_render_f64(const oracle_scene* scene, const float* frame96, const oracle_params* params, float* rgba32f,
                       double* accum, oracle_stats* stats);
 void oracle_rand(float cx, float cy, float salt, int trig_mode, int n, float* out);

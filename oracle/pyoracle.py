@@ -142,6 +142,26 @@ def render(sc, frame, prm: OParams, tri_bvh=None, sphere_bvh=None):
             "stats": {k: int(getattr(st, k)) for k in STATS_FIELDS}}
 
 
+def render_f64(sc, frame, prm: OParams, tri_bvh=None, sphere_bvh=None):
+    """FP64 evaluation of the same paths (RNG in float): returns dict(lin =
+    mean radiance (h, w, 3), image = tonemap(lin) + dither in double)."""
+    L = lib()
+    ref = _SceneRef(sc, tri_bvh, sphere_bvh)
+    f = np.ascontiguousarray(frame).reshape(())
+    h, w = prm.height, prm.width
+    rgba = np.zeros((h, w, 4), np.float32)
+    acc = np.zeros((h, w, 4), np.float64)
+    st = OStats()
+    L.oracle_render_f64(ctypes.byref(ref.s), f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(prm), _p(rgba), _p(acc),
+                        ctypes.byref(st))
+    lin = acc[..., :3]
+    x = lin / (lin + 1.0)
+    gamma = np.float64(np.float32(1.0) / np.float32(2.2))  # the shader's 1.0 / 2.2 in float
+    with np.errstate(invalid="ignore"):
+        img = np.power(x, gamma)
+    return {"lin": lin, "image": img + acc[..., 3:4], "rgba32f": rgba}
+
+
 def rand(cx, cy, salt, n, trig_mode=0):
     out = np.zeros(n, np.float32)
     lib().oracle_rand(cx, cy, salt, trig_mode, n, _p(out))

@@ -732,6 +732,7 @@ template <class T> static void shade_pixel(Tracer<T>& tr, const Frame<T>& fr, co
     accum = accum / (accum + splat(T(1)));
     accum = vpow(accum, T(1.0f / 2.2f));
     const T dither = T(rand(g)) / T(64);
+    if (accum_out) accum_out[3] = dither;
     rgba[0] = (float)(accum.x + dither);
     rgba[1] = (float)(accum.y + dither);
     rgba[2] = (float)(accum.z + dither);
@@ -788,7 +789,7 @@ static int render(const oracle_scene* sd, const float* frame, const oracle_param
                 float rgba[4];
                 uint32_t prim = 0xFFFFFFFFu;
                 float t0 = -1.0f;
-                T acc3[3];
+                T acc3[4];
                 shade_pixel(tr, fr, p, x, y, rgba, &prim, &t0, acc3);
                 if (rgba32f) std::memcpy(rgba32f + 4 * i, rgba, 16);
                 if (rgba8)
@@ -796,7 +797,7 @@ static int render(const oracle_scene* sd, const float* frame, const oracle_param
                 if (hit_id) hit_id[i] = prim;
                 if (hit_t) hit_t[i] = t0;
                 if (accum)
-                    for (int c = 0; c < 3; ++c) accum[3 * i + c] = (double)acc3[c];
+                    for (int c = 0; c < 4; ++c) accum[4 * i + c] = (double)acc3[c];
             }
         }
     }

@@ -43,6 +43,15 @@ def gpu_tracer(tracer_lib):
     t.close()
 
 
+def fbits(a):
+    """float32 bit patterns with every NaN mapped to one canonical NaN: the
+    payload an operation returns for NaN operands depends on the operand
+    order a compiler picks for commutative + and *, and carries no meaning."""
+    import numpy as np
+    a = np.ascontiguousarray(a, np.float32)
+    return np.where(np.isnan(a), np.uint32(0x7FC00000), a.view(np.uint32))
+
+
 def golden(name):
     import numpy as np
     return np.load(os.path.join(GOLDEN, name), allow_pickle=False)

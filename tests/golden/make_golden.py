@@ -38,6 +38,11 @@ CROPS = [(0, 0), (0, 480), (500, 500), (992, 992), (300, 10)]  # (y, x) of 32x32
 
 
 def sha(a: np.ndarray) -> str:
+    """SHA-256 of the array's bytes; float32 NaNs are first mapped to one
+    canonical NaN (their payload depends on compiler operand order)."""
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.float32:
+        a = np.where(np.isnan(a), np.uint32(0x7FC00000), a.view(np.uint32))
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 

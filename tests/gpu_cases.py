@@ -3,6 +3,8 @@ from __future__ import annotations
 
 import numpy as np
 
+from conftest import fbits
+
 import pyoracle
 from vktrace import abi
 from vktrace import scene as S
@@ -81,7 +83,7 @@ def compare(gpu, ora, check_stats=True):
     assert e <= IMAGE_RMSE_TOL, f"image RMSE {e}"
     # column 0: NaN exactly where the oracle has NaN
     assert np.array_equal(np.isnan(gpu["rgba32f"][:, 0]), np.isnan(ora["rgba32f"][:, 0]))
-    exact = float(np.mean(np.all(gpu["rgba32f"].view(np.uint32) == ora["rgba32f"].view(np.uint32), axis=-1)))
+    exact = float(np.mean(np.all(fbits(gpu["rgba32f"]) == fbits(ora["rgba32f"]), axis=-1)))
     if check_stats and "stats" in gpu:
         if gpu["kernel"] == abi.KERNEL_PLAIN:
             # the plain kernel visits nodes in the oracle's order: every counter equal

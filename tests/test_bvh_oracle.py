@@ -2,6 +2,8 @@
 import numpy as np
 import pytest
 
+from conftest import fbits
+
 from vktrace import abi, configs
 from vktrace import scene as S
 
@@ -51,7 +53,7 @@ def test_oracle_bvh_equals_linear_strict(oracle_lib, tracer_lib, seed):
     prm = oracle_lib.params(48, 40, spp=2, max_depth=5, rr_start=2, sky=(1.0, 0.9, 0.8), tie_mode=1)
     a = oracle_lib.render(sc, fr, prm)
     b = oracle_lib.render(sc, fr, prm, tri_bvh=tb, sphere_bvh=sb)
-    assert np.array_equal(a["rgba32f"].view(np.uint32), b["rgba32f"].view(np.uint32))
+    assert np.array_equal(fbits(a["rgba32f"]), fbits(b["rgba32f"]))
     assert np.array_equal(a["hit_id"], b["hit_id"])
     assert a["stats"]["closest_rays"] == b["stats"]["closest_rays"]
     assert b["stats"]["node_fetches"] > 0 and b["stats"]["tri_tests"] < a["stats"]["tri_tests"]

@@ -5,6 +5,8 @@ baseline must equal both."""
 import numpy as np
 import pytest
 
+from conftest import fbits
+
 from gpu_cases import compare, run_oracle, scene_bvhs, soup_scene, sphere_scene
 from vktrace import abi
 from vktrace import scene as S
@@ -39,7 +41,7 @@ def _single(tr, sc, fr, p):
 
 
 def _bits(a):
-    return np.ascontiguousarray(a).view(np.uint32)
+    return fbits(a)
 
 
 def test_batched_equals_single_scene(gpu_tracer):

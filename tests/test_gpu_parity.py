@@ -7,6 +7,8 @@ sample counts; the ray / node / primitive-test counters equal the oracle's.
 import numpy as np
 import pytest
 
+from conftest import fbits
+
 from gpu_cases import compare, run_gpu, run_oracle, soup_scene, sphere_scene
 from vktrace import abi
 from vktrace import scene as S
@@ -71,7 +73,7 @@ def test_kernels_identical(gpu_tracer):
     fr = S.frame(S.look_at((0.0, 5.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.3)
     a = run_gpu(gpu_tracer, sc, fr, 77, 61, 3, 6, rr_start=2, sky=(0.8, 0.9, 1.0), kernel=abi.KERNEL_PLAIN)
     b = run_gpu(gpu_tracer, sc, fr, 77, 61, 3, 6, rr_start=2, sky=(0.8, 0.9, 1.0), kernel=abi.KERNEL_WAVEFRONT)
-    assert np.array_equal(a["rgba32f"].view(np.uint32), b["rgba32f"].view(np.uint32))
+    assert np.array_equal(fbits(a["rgba32f"]), fbits(b["rgba32f"]))
     assert np.array_equal(a["rgba8"], b["rgba8"])
     assert np.array_equal(a["hit_id"], b["hit_id"])
     for k in ("closest_rays", "shadow_rays", "hits"):
@@ -86,7 +88,7 @@ def test_bvh_equals_linear_strict(gpu_tracer):
     a = run_gpu(gpu_tracer, sc, fr, 64, 64, 2, 4, sky=(1, 1, 1), stats=False)
     lin = S.Scene(triangles=sc.triangles, materials=sc.materials, bvh=S.BVH_NONE)
     b = run_gpu(gpu_tracer, lin, fr, 64, 64, 2, 4, sky=(1, 1, 1), stats=False)
-    assert np.array_equal(a["rgba32f"].view(np.uint32), b["rgba32f"].view(np.uint32))
+    assert np.array_equal(fbits(a["rgba32f"]), fbits(b["rgba32f"]))
     assert np.array_equal(a["hit_id"], b["hit_id"])
 
 

@@ -63,6 +63,17 @@ struct SceneBuffers {
     }
 };
 
+struct AdjBuffers {
+    DevBuf<float4> dldi, lin;
+    DevBuf<float> grad;
+    void release()
+    {
+        dldi.release();
+        lin.release();
+        grad.release();
+    }
+};
+
 }  // namespace
 
 struct tracer_ctx {
@@ -79,6 +90,7 @@ struct tracer_ctx {
     DevBuf<uchar4> rgba8;
     DevBuf<float4> rgba32f;
     DevBuf<uint2> hit;
+    DevBuf<float4> linear;
     DevBuf<unsigned long long> stats;
     DevBuf<int> status;
     uint32_t last_mask = 0;
@@ -112,6 +124,7 @@ struct tracer_ctx {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<uint64_t> graph_key;
+    AdjBuffers adj;  // adjoint: dL/dI, linear image and gradient buffers
 };
 
 namespace {
@@ -356,6 +369,7 @@ void tracer_destroy(tracer_ctx* c)
     if (c->pending && c->done) wait_event(c, c->done);
     c->scene.release();
     c->batch.release();
+    c->adj.release();
     c->batch_slots.release();
     c->b_rgba8.release();
     c->b_rgba32f.release();
@@ -366,6 +380,7 @@ void tracer_destroy(tracer_ctx* c)
     c->rgba8.release();
     c->rgba32f.release();
     c->hit.release();
+    c->linear.release();
     c->stats.release();
     c->status.release();
     release_wavefront(c);
@@ -520,7 +535,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
     const uint32_t mask = p->aov_mask ? p->aov_mask : (1u << TRACER_AOV_RGBA8);
     if (mask & ~((1u << TRACER_AOV_RGBA8) | (1u << TRACER_AOV_RGBA32F) | (1u << TRACER_AOV_PRIMARY_HIT) |
-                 (1u << TRACER_AOV_STATS)))
+                 (1u << TRACER_AOV_STATS) | (1u << TRACER_AOV_LINEAR)))
         return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "unknown AOV in mask 0x%x", mask);
 
     int r = finish(c);
@@ -531,6 +546,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     if (mask & (1u << TRACER_AOV_RGBA8)) e = dalloc(c->rgba8, npx);
     if (e == cudaSuccess && (mask & (1u << TRACER_AOV_RGBA32F))) e = dalloc(c->rgba32f, npx);
     if (e == cudaSuccess && (mask & (1u << TRACER_AOV_PRIMARY_HIT))) e = dalloc(c->hit, npx);
+    if (e == cudaSuccess && (mask & (1u << TRACER_AOV_LINEAR))) e = dalloc(c->linear, npx);
     if (e != cudaSuccess) return cuda_fail(c, e, "image allocation");
     c->width = p->width;
     c->height = p->height;
@@ -561,6 +577,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     a.rgba8 = (mask & (1u << TRACER_AOV_RGBA8)) ? c->rgba8.p : nullptr;
     a.rgba32f = (mask & (1u << TRACER_AOV_RGBA32F)) ? c->rgba32f.p : nullptr;
     a.hit = (mask & (1u << TRACER_AOV_PRIMARY_HIT)) ? c->hit.p : nullptr;
+    a.linear = (mask & (1u << TRACER_AOV_LINEAR)) ? c->linear.p : nullptr;
     a.stats = c->stats.p;
     a.status = c->status.p;
     const int stats = (p->stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
@@ -647,6 +664,7 @@ static int aov_info(tracer_ctx* c, int aov, void** ptr, size_t* bytes)
     case TRACER_AOV_RGBA8: *ptr = c->rgba8.p; *bytes = npx * 4; break;
     case TRACER_AOV_RGBA32F: *ptr = c->rgba32f.p; *bytes = npx * 16; break;
     case TRACER_AOV_PRIMARY_HIT: *ptr = c->hit.p; *bytes = npx * 8; break;
+    case TRACER_AOV_LINEAR: *ptr = c->linear.p; *bytes = npx * 16; break;
     case TRACER_AOV_STATS: *ptr = c->stats.p; *bytes = sizeof(tracer_stats); break;
     default: return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "unknown AOV %d", aov);
     }
@@ -1227,5 +1245,132 @@ extern "C" int tracer_readback_scene(tracer_ctx* c, uint32_t scene, int aov, voi
                                 scene, n, bytes);
     cudaError_t e = cudaMemcpy(dst, src, n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(c, e, "readback");
+    return TRACER_OK;
+}
+
+// ------------------------------------------------------------------ adjoint
+namespace {
+
+bool is_device_ptr(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // an unregistered host pointer is not an error
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+
+}  // namespace
+
+extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params* p,
+                                    const float* dL_dimage, const float* linear_image, float* d_albedo,
+                                    float* d_emission, float* d_campos, void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!f || !p || !dL_dimage) return fail(c, TRACER_ERR_INVALID_ARG, "null frame, params or dL/dI");
+    if (!c->scene.loaded) return fail(c, TRACER_ERR_NO_SCENE, "no scene uploaded");
+    if (p->width == 0 || p->height == 0 || p->width > 32768 || p->height > 32768)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "image size %ux%u not supported", p->width, p->height);
+    if (p->spp == 0 || p->max_depth == 0 || p->max_depth > 1024 || p->spp > 1u << 20)
+        return fail(c, TRACER_ERR_INVALID_ARG, "spp %u / max_depth %u out of range", p->spp, p->max_depth);
+    if (p->tie_mode != TRACER_TIES_REFERENCE && p->tie_mode != TRACER_TIES_STRICT)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
+    if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
+        return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
+    const SceneBuffers& s = c->scene;
+    const uint32_t need = s.bvh ? (s.depth > 1 ? s.depth : 1) : 0;
+    const uint32_t stack = p->stack_depth ? p->stack_depth : need;
+    if (s.bvh && stack < need)
+        return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
+    if ((size_t)stack * 128 * 8 > 100 * 1024)
+        return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    AdjBuffers& ab = c->adj;
+    const size_t npx = (size_t)p->width * p->height;
+    const size_t ng = 6 * (size_t)s.nm + 3;
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    cudaError_t e = dalloc(ab.grad, ng);
+    const float4* dldi = reinterpret_cast<const float4*>(dL_dimage);
+    if (e == cudaSuccess && !is_device_ptr(dL_dimage)) {
+        e = dalloc(ab.dldi, npx);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ab.dldi.p, dL_dimage, npx * 16, cudaMemcpyHostToDevice, st);
+        dldi = ab.dldi.p;
+    }
+    const float4* lin = reinterpret_cast<const float4*>(linear_image);
+    if (e == cudaSuccess && linear_image && !is_device_ptr(linear_image)) {
+        e = dalloc(ab.lin, npx);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ab.lin.p, linear_image, npx * 16, cudaMemcpyHostToDevice, st);
+        lin = ab.lin.p;
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(ab.grad.p, 0, ng * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint set-up");
+
+    TraceArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
+                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes};
+    a.fr.aspect = f->aspect_ratio;
+    a.fr.seed = f->seed;
+    a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
+    a.fr.cdir = V3{f->camera.dir[0], f->camera.dir[1], f->camera.dir[2]};
+    a.fr.cright = V3{f->camera.right[0], f->camera.right[1], f->camera.right[2]};
+    a.fr.cup = V3{f->camera.up[0], f->camera.up[1], f->camera.up[2]};
+    a.width = p->width;
+    a.height = p->height;
+    a.spp = p->spp;
+    a.max_depth = p->max_depth;
+    a.rr_start = p->rr_start;
+    a.sky = V3{p->sky[0], p->sky[1], p->sky[2]};
+    a.sky_on = !(p->sky[0] == 0.0f && p->sky[1] == 0.0f && p->sky[2] == 0.0f);
+    a.stack_depth = stack;
+    const uint32_t nn = s.n_tri_nodes > s.n_sph_nodes ? s.n_tri_nodes : s.n_sph_nodes;
+    a.trav_limit = 2 * nn + 16;
+    a.stats = c->stats.p;
+    a.status = c->status.p;
+    c->last_kernel = 3;
+    c->last_rounds = 0;
+    c->last_prof_rounds = 0;
+    c->last_launches = 1;
+    c->last_mask = 1u << TRACER_AOV_STATS;
+    c->width = p->width;
+    c->height = p->height;
+    if (c->profiling) cudaEventRecord(c->prof_begin, st);
+    e = launch_adjoint(a, dldi, lin, ab.grad.p, s.nm, p->tie_mode, s.bvh ? 1 : 0, st);
+    if (c->profiling) cudaEventRecord(c->prof_end, st);
+    if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint launch");
+    c->pending = true;
+    // outputs: device pointers get asynchronous copies, host pointers wait
+    float* outs[3] = {d_albedo, d_emission, d_campos};
+    const size_t offs[3] = {0, 3 * (size_t)s.nm, 6 * (size_t)s.nm};
+    const size_t lens[3] = {3 * (size_t)s.nm, 3 * (size_t)s.nm, 3};
+    bool host_out = false;
+    for (int k = 0; k < 3; ++k) {
+        if (!outs[k]) continue;
+        if (is_device_ptr(outs[k])) {
+            e = cudaMemcpyAsync(outs[k], ab.grad.p + offs[k], lens[k] * sizeof(float), cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return cuda_fail(c, e, "gradient copy");
+        } else {
+            host_out = true;
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint completion event");
+    if (host_out) {
+        r = finish(c);
+        if (r != TRACER_OK) return r;
+        for (int k = 0; k < 3; ++k)
+            if (outs[k] && !is_device_ptr(outs[k])) {
+                e = cudaMemcpy(outs[k], ab.grad.p + offs[k], lens[k] * sizeof(float), cudaMemcpyDeviceToHost);
+                if (e != cudaSuccess) return cuda_fail(c, e, "gradient readback");
+            }
+    }
     return TRACER_OK;
 }

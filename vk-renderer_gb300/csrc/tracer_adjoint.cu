@@ -1,0 +1,433 @@
+// Adjoint (reverse-mode) trace for sm_103a: gradients of an image loss with
+// respect to the material table's albedo and emission and to the camera
+// position, by path replay with O(1) state per path (no stored path vertices).
+//
+// The image is I = tonemap(accum / spp) + dither (Tracer.comp:585-590), accum
+// the sum of the samples' radiance (:578-581).  Given dL/dI per pixel:
+//   delta = dL/dI * tonemap'(accum / spp) / spp               (per channel)
+// and for every sample, replaying its path twice from the sample's RNG state:
+//   pass 1 (primal): the radiance loop (:433-553) as in the forward kernels,
+//     recording per channel the last depth at which the clamp of acc
+//     (:441) was active -- contributions before it do not reach the output --
+//     and the sum T of the contributions that do;
+//   pass 2 (adjoint): the same path again.  At a bounce k on material m:
+//     emission:  d/de_m of the contribution added at k (normalize(e) for
+//                diffuse, :507; e * mask for dielectric, :516);
+//     albedo:    every later contribution is proportional to a_m (mask *=
+//                albedo, :510/:517), so d/da_m[c] += delta[c] * R[c] / a_m[c]
+//                with R = T - (surviving contributions up to k) ("remaining
+//                radiance", path replay backpropagation, Vicini et al. 2021);
+//                plus the direct dependence of next-event estimation on the
+//                albedo at k (kD * albedo / pi and F0 = mix(0.04, albedo,
+//                metalness), :481-502);
+//     camera:    forward-mode tangents of each ray's origin and direction with
+//                respect to the camera position (the primary ray starts at
+//                it, :574) carried through every hit, scatter and next-event
+//                estimate; the camera enters radiance only through next-event
+//                estimation (hit points, the light's cone, V = normalize(
+//                camera.pos - P), :464-502).
+// Discrete decisions (which primitive is hit, shadow visibility, dielectric
+// reflect/refract choice, Russian-roulette survival) are those of the path;
+// the Russian-roulette normalisation mask /= max3(mask) is treated as a
+// constant (the gradient of the expected value; it has no effect on any
+// contribution when roulette only runs at the last depth).  Gradients are
+// reduced per block in shared memory and added to global memory once per block.
+
+#include <cuda_runtime.h>
+
+#include "tracer_core.cuh"
+#include "tracer_launch.h"
+
+namespace vkt {
+
+// --------------------------------------------------------- JVP helpers --
+__device__ __forceinline__ V3 dnorm(V3 x, V3 dx)
+{
+    const float il = 1.0f / sqrtf(dot(x, x));
+    const V3 y = x * il;
+    return (dx - y * dot(y, dx)) * il;
+}
+__device__ __forceinline__ V3 dcross(V3 a, V3 da, V3 b, V3 db) { return cross(da, b) + cross(a, db); }
+__device__ __forceinline__ V3 dreflect(V3 I, V3 dI, V3 N, V3 dN)
+{
+    const float ni = dot(N, I);
+    const float dni = dot(dN, I) + dot(N, dI);
+    return dI - dN * (2.0f * ni) - N * (2.0f * dni);
+}
+__device__ __forceinline__ V3 drefract(V3 I, V3 dI, V3 N, V3 dN, float eta)
+{
+    const float d = dot(N, I);
+    const float dd = dot(dN, I) + dot(N, dI);
+    const float k = 1.0f - eta * eta * (1.0f - d * d);
+    const float sk = sqrtf(k);
+    const float dk = 2.0f * eta * eta * d * dd;
+    return dI * eta - N * (eta * dd + dk / (2.0f * sk)) - dN * (eta * d + sk);
+}
+// d jitter(d, phi, sina, cosa) for varying d, sina, cosa (Tracer.comp:256-263)
+__device__ __forceinline__ V3 djitter(V3 d, V3 dd, float cphi, float sphi, float sina, float dsina, float cosa,
+                                      float dcosa)
+{
+    const V3 w = normalize(d);
+    const V3 dw = dnorm(d, dd);
+    const V3 t = cross(v3(w.y, w.z, w.x), w);
+    const V3 dt = dcross(v3(w.y, w.z, w.x), v3(dw.y, dw.z, dw.x), w, dw);
+    const V3 u = normalize(t);
+    const V3 du = dnorm(t, dt);
+    const V3 v = cross(w, u);
+    const V3 dv = dcross(w, dw, u, du);
+    return (du * cphi + dv * sphi) * sina + (u * cphi + v * sphi) * dsina + dw * cosa + w * dcosa;
+}
+
+struct AdjArgs {
+    const float4* dldi;    // dL/dI per pixel (RGBA layout, alpha ignored)
+    const float4* linear;  // accum / spp per pixel from the forward trace, or NULL (recomputed)
+    float* grad;           // [nm x 3 albedo][nm x 3 emission][3 camera position]
+    uint32_t nm;
+    int smem_grad;         // reduce in shared memory first
+};
+
+__device__ __forceinline__ bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
+
+__device__ __forceinline__ void gadd(float* g, int i, float v)
+{
+    if (v != 0.0f && isfinite(v)) atomicAdd(g + i, v);
+}
+
+// One emitter's next-event estimate (same operations as nee_one) with its
+// derivative with respect to the albedo at this bounce (componentwise, de_da)
+// and, when CAM, with respect to the camera position (de_dc[j], j = x, y, z)
+// given the tangents dP, dN of the hit point and normal.
+template <bool CAM, class TR>
+__device__ __forceinline__ V3 nee_one_grad(TR& tr, const TraceArgs& a, uint32_t si, V3 P, V3 N, const V3* dP,
+                                           const V3* dN, const Material& mat, Rng& g, V3& de_da, V3* de_dc)
+{
+    const float4* rec = a.sc.sph_rec + 4 * (size_t)si;
+    const float4 geo = __ldg(rec + 3);
+    const V3 sP = v3(geo);
+    const float sr = geo.w;
+    const float t = length(sP - P) - sr;
+    const V3 l0 = sP - P;
+    const float ll = dot(l0, l0);
+    const float q = sr * sr / ll;
+    const float cos_a_max = sqrtf(1.0f - gclamp(q, 0.0f, 1.0f));
+    const float rho = rand01(g);
+    const float cosa = gmix(cos_a_max, 1.0f, rho);
+    const float phi = (2.0f * PI) * rand01(g);
+    const float sina = sqrtf(1.0f - cosa * cosa);
+    const V3 L = jitter(l0, phi, sina, cosa);
+    Hit sh;
+    sh.t = t;
+    if (tr.trace(Ray{P, L}, sh, true)) return splat(0.0f);
+    const float4 em = __ldg(rec + 1);
+    const float q2 = t / sr + 1.0f;
+    const V3 att1 = (v3(em) * 1.0f / (q2 * q2) - 0.001f) / (1.0f - 0.001f);
+    const V3 att = vmax0(att1);
+    V3 F0 = splat(0.04f);
+    F0 = vmix(F0, mat.albedo, mat.metalness);
+    const V3 V = normalize(a.fr.cpos - P);
+    const V3 H = normalize(V + L);
+    const float rough = mat.roughness;
+    const float ar = rough * rough, a2 = ar * ar;
+    const float nh = dot(N, H);
+    const float NdotH = gmax(nh, 0.0f);
+    const float dden = NdotH * NdotH * (a2 - 1.0f) + 1.0f;
+    const float NDF = a2 / (PI * dden * dden);
+    const float kg = (rough + 1.0f) * (rough + 1.0f) / 8.0f;
+    const float nv = dot(N, V), nl = dot(N, L);
+    const float NdotV = gmax(nv, 0.0f), NdotL = gmax(nl, 0.0f);
+    const float gv = NdotV / (NdotV * (1.0f - kg) + kg), gl = NdotL / (NdotL * (1.0f - kg) + kg);
+    const float G = gl * gv;
+    const float hv = dot(H, V);
+    const float cth = gmax(hv, 0.0f);
+    const float s5 = powf(1.0f - cth, 5.0f);
+    const V3 F = F0 + (1.0f - F0) * s5;
+    const V3 kD = (1.0f - F) * (1.0f - mat.metalness);
+    const float den4 = 4.0f * NdotV * NdotL;
+    const float D = gmax(den4, 0.001f);
+    const V3 spec = NDF * G * F / D;
+    const V3 base = kD * mat.albedo / PI + spec;
+    // d/d albedo (componentwise): dF/da = metal (1 - s5); dkD/da = -dF/da (1 - metal)
+    {
+        const float dFda = mat.metalness * (1.0f - s5);
+        const float dkDda = -dFda * (1.0f - mat.metalness);
+        const V3 dbase = (dkDda * mat.albedo + kD) / PI + splat(NDF * G * dFda / D);
+        de_da = de_da + dbase * att * NdotL;
+    }
+    if (CAM) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const V3 dl0 = splat(0.0f) - dP[j];
+            const float dt = dot(l0, dl0) / sqrtf(ll);
+            const float dq = (q > 0.0f && q < 1.0f) ? -sr * sr * 2.0f * dot(l0, dl0) / (ll * ll) : 0.0f;
+            const float dcm = cos_a_max > 0.0f ? -dq / (2.0f * cos_a_max) : 0.0f;
+            const float dcosa = (1.0f - rho) * dcm;
+            const float dsina = sina > 0.0f ? -cosa * dcosa / sina : 0.0f;
+            float cphi, sphi;
+            psincos(phi, sphi, cphi);
+            const V3 dL = djitter(l0, dl0, cphi, sphi, sina, dsina, cosa, dcosa);
+            const float dq2 = dt / sr;
+            V3 datt = v3(em) * (-2.0f * dq2 / (q2 * q2 * q2)) / (1.0f - 0.001f);
+            datt = v3(att1.x > 0.0f ? datt.x : 0.0f, att1.y > 0.0f ? datt.y : 0.0f, att1.z > 0.0f ? datt.z : 0.0f);
+            const V3 ej = v3(j == 0 ? 1.0f : 0.0f, j == 1 ? 1.0f : 0.0f, j == 2 ? 1.0f : 0.0f);
+            const V3 dV = dnorm(a.fr.cpos - P, ej - dP[j]);
+            const V3 dH = dnorm(V + L, dV + dL);
+            const float dNdotH = nh > 0.0f ? dot(dN[j], H) + dot(N, dH) : 0.0f;
+            const float dNDF = -2.0f * a2 / (PI * dden * dden * dden) * (2.0f * NdotH * (a2 - 1.0f) * dNdotH);
+            const float dNdotV = nv > 0.0f ? dot(dN[j], V) + dot(N, dV) : 0.0f;
+            const float dNdotL = nl > 0.0f ? dot(dN[j], L) + dot(N, dL) : 0.0f;
+            const float cv = NdotV * (1.0f - kg) + kg, cl = NdotL * (1.0f - kg) + kg;
+            const float dG = kg / (cl * cl) * dNdotL * gv + gl * kg / (cv * cv) * dNdotV;
+            const float dcth = hv > 0.0f ? dot(dH, V) + dot(H, dV) : 0.0f;
+            const float om = 1.0f - cth;
+            const float ds5 = -5.0f * om * om * om * om * dcth;
+            const V3 dF = (1.0f - F0) * ds5;
+            const V3 dkD = splat(0.0f) - dF * (1.0f - mat.metalness);
+            const float dD = den4 > 0.001f ? 4.0f * (dNdotV * NdotL + NdotV * dNdotL) : 0.0f;
+            const V3 dspec = (dNDF * G * F + NDF * dG * F + NDF * G * dF) / D - spec * (dD / D);
+            const V3 dbase = dkD * mat.albedo / PI + dspec;
+            de_dc[j] = de_dc[j] + (dbase * att + base * datt) * NdotL + base * att * dNdotL;
+        }
+    }
+    return base * att * NdotL;
+}
+
+// Pass 1: the radiance loop with clamp bookkeeping.  lc[c] = last depth whose
+// clamp of acc[c] was active (-1: none); T = contributions that survive.
+template <class TR>
+__device__ __forceinline__ void primal_pass(TR& tr, const TraceArgs& a, Ray ray, Rng& g, int* lc, V3& T)
+{
+    V3 acc = splat(0.0f), mask = splat(1.0f);
+    T = splat(0.0f);
+    for (uint32_t depth = 0; depth < a.max_depth; ++depth) {
+        if (acc.x < 0.0f || acc.x > 1.0f) { lc[0] = (int)depth; T.x = 0.0f; }
+        if (acc.y < 0.0f || acc.y > 1.0f) { lc[1] = (int)depth; T.y = 0.0f; }
+        if (acc.z < 0.0f || acc.z > 1.0f) { lc[2] = (int)depth; T.z = 0.0f; }
+        acc = vclamp01(acc);
+        Hit h;
+        h.t = depth_tmax(depth);
+        const bool found = tr.trace(ray, h, false);
+        const V3 before = acc;
+        const bool cont = shade_bounce(tr, a, depth, found, h, ray, acc, mask, g);
+        T = T + (acc - before);
+        if (!cont) break;
+    }
+}
+
+template <int TIE, bool BVH, bool CAM>
+__global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
+{
+    extern __shared__ int smem[];
+    const int tid = threadIdx.x, nthreads = blockDim.x;
+    const Stack stk{smem + tid, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * nthreads) + tid, nthreads,
+                    (int)a.stack_depth};
+    float* sgrad = reinterpret_cast<float*>(smem + 2 * (size_t)a.stack_depth * nthreads);
+    const uint32_t ngrad = 6 * ga.nm + 3;
+    if (ga.smem_grad) {
+        for (uint32_t k = tid; k < ngrad; k += nthreads) sgrad[k] = 0.0f;
+        __syncthreads();
+    }
+    float* grad = ga.smem_grad ? sgrad : ga.grad;
+    float* gal = grad;
+    float* gem = grad + 3 * ga.nm;
+    float* gcam = grad + 6 * ga.nm;
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    Tracer<TIE, BVH, true> tr{a.sc, stk, cnt, a.status, a.trav_limit};
+    const uint32_t x = blockIdx.x * 16 + (tid & 15);
+    const uint32_t y = blockIdx.y * (nthreads >> 4) + (tid >> 4);
+    if (x < a.width && y < a.height) {
+        const size_t i = (size_t)y * a.width + x;
+        Rng g;
+        seed_rng(a, x, y, g);
+        const Ray pr = primary_ray(a, x, y);
+        V3 lin;
+        if (ga.linear) {
+            lin = v3(ga.linear[i]);
+        } else {
+            Rng g0 = g;
+            V3 acc = splat(0.0f);
+            for (uint32_t s = 0; s < a.spp; ++s) acc = acc + radiance(tr, a, pr, g0, nullptr, nullptr);
+            lin = acc / (float)a.spp;
+        }
+        const float4 dl = ga.dldi[i];
+        // tonemap(x) = (x / (x + 1))^(1/2.2): slope g (x/(x+1))^(g-1) / (x+1)^2
+        // (infinite at 0: the slope is taken at x >= 1e-6)
+        const float gam = 1.0f / 2.2f;
+        auto tm_slope = [&](float xx) {
+            xx = gmax(xx, 1e-6f);
+            const float r = xx / (xx + 1.0f);
+            return gam * powf(r, gam - 1.0f) / ((xx + 1.0f) * (xx + 1.0f));
+        };
+        const V3 delta = v3(dl.x * tm_slope(lin.x), dl.y * tm_slope(lin.y), dl.z * tm_slope(lin.z)) / (float)a.spp;
+        if (finite3(delta) && finite3(lin)) {
+            for (uint32_t s = 0; s < a.spp; ++s) {
+                const Rng gs = g;  // this sample's RNG state
+                int lc[3] = {-1, -1, -1};
+                V3 T;
+                primal_pass(tr, a, pr, g, lc, T);  // advances g past the sample
+                // pass 2: adjoint replay
+                Rng g2 = gs;
+                V3 mask = splat(1.0f), prefix = splat(0.0f);
+                Ray ray = pr;
+                V3 dO[3], dD[3];
+                if (CAM) {
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        dO[j] = v3(j == 0 ? 1.0f : 0.0f, j == 1 ? 1.0f : 0.0f, j == 2 ? 1.0f : 0.0f);
+                        dD[j] = splat(0.0f);
+                    }
+                }
+                for (uint32_t depth = 0; depth < a.max_depth; ++depth) {
+                    Hit h;
+                    h.t = depth_tmax(depth);
+                    const bool found = tr.trace(ray, h, false);
+                    const V3 surv = v3((int)depth >= lc[0] ? 1.0f : 0.0f, (int)depth >= lc[1] ? 1.0f : 0.0f,
+                                       (int)depth >= lc[2] ? 1.0f : 0.0f);
+                    const V3 w = delta * surv;
+                    if (!found) {
+                        if (a.sky_on) prefix = prefix + mask * a.sky * surv;
+                        break;
+                    }
+                    V3 P, N;
+                    Material mat;
+                    tr.surface(ray, h, P, N, mat);
+                    const int m = h.kind == 1 ? (int)__float_as_uint(__ldg(a.sc.tri + 3 * (size_t)h.slot).w) : -1;
+                    V3 dP[3], dN[3];
+                    if (CAM) {
+                        const float nd = dot(N, ray.d);
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) {
+                            const V3 q = dO[j] + dD[j] * h.t;
+                            const float dt = -dot(N, q) / nd;
+                            dP[j] = q + ray.d * dt;
+                            dN[j] = h.kind == 2 ? dP[j] / __ldg(a.sc.sph_geo + h.slot).w : splat(0.0f);
+                        }
+                    }
+                    V3 C = splat(0.0f);
+                    if (mat.type == MAT_DIFFUSE) {
+                        const float r2 = rand01(g2);
+                        const float phi = (2.0f * PI) * rand01(g2);
+                        const float sa = sqrtf(r2), ca = sqrtf(1.0f - r2);
+                        const V3 jd = jitter(N, phi, sa, ca);
+                        const V3 d = jd * (1.0f - mat.metalness);
+                        V3 e = splat(0.0f), de_da = splat(0.0f);
+                        V3 de_dc[3] = {splat(0.0f), splat(0.0f), splat(0.0f)};
+                        for (uint32_t k = 0; k < a.sc.ne; ++k)
+                            e = e + nee_one_grad<CAM>(tr, a, __ldg(a.sc.emit + k), P, N, dP, dN, mat, g2, de_da, de_dc);
+                        const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
+                        const V3 en = emits ? normalize(mat.emissive) : splat(0.0f);
+                        C = mask * (en + e);
+                        const V3 wm = w * mask;
+                        if (m >= 0) {
+                            if (emits) {  // d normalize(e) = (I - n n^T) / |e|
+                                const float il = 1.0f / length(mat.emissive);
+                                const V3 ge = (wm - en * dot(en, wm)) * il;
+                                gadd(gem, 3 * m + 0, ge.x);
+                                gadd(gem, 3 * m + 1, ge.y);
+                                gadd(gem, 3 * m + 2, ge.z);
+                            }
+                            const V3 gd = wm * de_da;
+                            gadd(gal, 3 * m + 0, gd.x);
+                            gadd(gal, 3 * m + 1, gd.y);
+                            gadd(gal, 3 * m + 2, gd.z);
+                        }
+                        if (CAM) {
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) gadd(gcam, j, dot(wm, de_dc[j]));
+                        }
+                        prefix = prefix + C * surv;
+                        if (m >= 0) {
+                            const V3 R = T - prefix;
+                            if (mat.albedo.x != 0.0f) gadd(gal, 3 * m + 0, delta.x * R.x / mat.albedo.x);
+                            if (mat.albedo.y != 0.0f) gadd(gal, 3 * m + 1, delta.y * R.y / mat.albedo.y);
+                            if (mat.albedo.z != 0.0f) gadd(gal, 3 * m + 2, delta.z * R.z / mat.albedo.z);
+                        }
+                        mask = mask * mat.albedo;
+                        const V3 rf = reflect(ray.d, N);
+                        if (CAM) {
+                            float cphi, sphi;
+                            psincos(phi, sphi, cphi);
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) {
+                                const V3 djd = djitter(N, dN[j], cphi, sphi, sa, 0.0f, ca, 0.0f);
+                                const V3 drf = dreflect(ray.d, dD[j], N, dN[j]);
+                                dD[j] = dnorm(rf + d, drf + djd * (1.0f - mat.metalness));
+                                dO[j] = dP[j];
+                            }
+                        }
+                        ray = Ray{P, normalize(rf + d)};
+                    } else if (mat.type == MAT_DIELECTRIC) {
+                        C = mat.emissive * mask;
+                        if (m >= 0) {
+                            const V3 ge = w * mask;
+                            gadd(gem, 3 * m + 0, ge.x);
+                            gadd(gem, 3 * m + 1, ge.y);
+                            gadd(gem, 3 * m + 2, ge.z);
+                        }
+                        prefix = prefix + C * surv;
+                        if (m >= 0) {
+                            const V3 R = T - prefix;
+                            if (mat.albedo.x != 0.0f) gadd(gal, 3 * m + 0, delta.x * R.x / mat.albedo.x);
+                            if (mat.albedo.y != 0.0f) gadd(gal, 3 * m + 1, delta.y * R.y / mat.albedo.y);
+                            if (mat.albedo.z != 0.0f) gadd(gal, 3 * m + 2, delta.z * R.z / mat.albedo.z);
+                        }
+                        mask = mask * mat.albedo;
+                        const float cosine = -dot(ray.d, N) / length(ray.d);
+                        const V3 reflected = reflect(ray.d, N);
+                        const V3 refracted = refract(ray.d, N, mat.roughness);
+                        const bool tir = refracted == splat(0.0f);
+                        const float prob = tir ? 1.0f : schlick(cosine, mat.roughness);
+                        const bool refl = rand01(g2) < prob;
+                        const V3 nd = refl ? reflected : refracted;
+                        if (CAM) {
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) {
+                                const V3 dr = refl ? dreflect(ray.d, dD[j], N, dN[j])
+                                                   : drefract(ray.d, dD[j], N, dN[j], mat.roughness);
+                                dD[j] = dnorm(nd, dr);
+                                dO[j] = dP[j];
+                            }
+                        }
+                        ray = Ray{P, normalize(nd)};
+                    }
+                    if (depth >= a.rr_start) {
+                        const float p = max3(mask);
+                        if (rand01(g2) > p) break;
+                        mask = mask * (1.0f / p);
+                    }
+                }
+            }
+        }
+    }
+    flush_counters(a, cnt);
+    if (ga.smem_grad) {
+        __syncthreads();
+        for (uint32_t k = tid; k < ngrad; k += nthreads)
+            if (sgrad[k] != 0.0f) atomicAdd(ga.grad + k, sgrad[k]);
+    }
+}
+
+template <int TIE, bool BVH, bool CAM>
+static cudaError_t adj_t(const TraceArgs& a, const AdjArgs& g, cudaStream_t s)
+{
+    const uint32_t block = 128;
+    const size_t smem = (size_t)a.stack_depth * block * 8 + (g.smem_grad ? (6 * (size_t)g.nm + 3) * 4 : 0);
+    auto k = k_adjoint<TIE, BVH, CAM>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((a.width + 15) / 16, (a.height + (block / 16) - 1) / (block / 16));
+    k<<<grid, block, smem, s>>>(a, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, float* grad, uint32_t nm,
+                           int tie, int bvh, cudaStream_t s)
+{
+    AdjArgs g{dldi, linear, grad, nm, (6 * (size_t)nm + 3) * 4 <= 96 * 1024 ? 1 : 0};
+    const bool cam = a.sc.ne > 0;
+    if (tie == TIE_REFERENCE) return cam ? adj_t<TIE_REFERENCE, false, true>(a, g, s) : adj_t<TIE_REFERENCE, false, false>(a, g, s);
+    if (bvh) return cam ? adj_t<TIE_STRICT, true, true>(a, g, s) : adj_t<TIE_STRICT, true, false>(a, g, s);
+    return cam ? adj_t<TIE_STRICT, false, true>(a, g, s) : adj_t<TIE_STRICT, false, false>(a, g, s);
+}
+
+}  // namespace vkt

@@ -25,6 +25,7 @@ struct TraceArgs {
     uchar4* rgba8;
     float4* rgba32f;
     uint2* hit;
+    float4* linear;  // accum / spp before tone mapping (input of the adjoint)
     unsigned long long* stats;  // C_COUNT counters
     int* status;
     // wavefront: first global path slot of this scene's pixels, and (in the
@@ -419,6 +420,7 @@ __device__ __forceinline__ void resolve_pixel(const TraceArgs& a, uint32_t x, ui
                                               uint32_t prim0, float t0)
 {
     accum = accum / (float)a.spp;
+    if (a.linear) a.linear[(size_t)y * a.width + x] = make_float4(accum.x, accum.y, accum.z, 1.0f);
     accum = accum / (accum + splat(1.0f));
     const float gam = 1.0f / 2.2f;
     accum = v3(powf(accum.x, gam), powf(accum.y, gam), powf(accum.z, gam));

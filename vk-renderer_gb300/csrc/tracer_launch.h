@@ -19,5 +19,7 @@ struct LaunchConfig {
 };
 
 cudaError_t launch_plain(const TraceArgs& a, const LaunchConfig& lc, cudaStream_t s);
+cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, float* grad, uint32_t nm,
+                           int tie, int bvh, cudaStream_t s);
 
 }  // namespace vkt

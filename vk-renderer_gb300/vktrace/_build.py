@@ -29,7 +29,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall"]
 
-SOURCES = ["tracer_kernels.cu", "tracer_wavefront.cu", "tracer_abi.cu", "bvh_build.cpp"]
+SOURCES = ["tracer_kernels.cu", "tracer_wavefront.cu", "tracer_adjoint.cu", "tracer_abi.cu", "bvh_build.cpp"]
 HEADERS = ["tracer_device.cuh", "tracer_core.cuh", "tracer_launch.h", "tracer_wavefront.h"]
 
 

@@ -29,7 +29,7 @@ ERR_BAD_BVH = -11
 
 TIES_REFERENCE, TIES_STRICT = 0, 1
 KERNEL_AUTO, KERNEL_PLAIN, KERNEL_WAVEFRONT = 0, 1, 2
-AOV_RGBA8, AOV_RGBA32F, AOV_PRIMARY_HIT, AOV_STATS = 0, 1, 2, 3
+AOV_RGBA8, AOV_RGBA32F, AOV_PRIMARY_HIT, AOV_STATS, AOV_LINEAR = 0, 1, 2, 3, 4
 PRIM_TRIANGLE, PRIM_SPHERE = 0, 1
 
 STATS_FIELDS = ["closest_rays", "shadow_rays", "node_fetches", "tri_tests", "sphere_tests", "plane_tests", "hits"]
@@ -39,7 +39,7 @@ EXPORTED_SYMBOLS = [
     "tracer_upload_scene", "tracer_set_materials", "tracer_trace", "tracer_readback", "tracer_synchronize",
     "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh", "tracer_set_profiling",
     "tracer_last_timings", "tracer_trace_noalloc", "tracer_upload_scenes", "tracer_trace_batched",
-    "tracer_readback_scene",
+    "tracer_readback_scene", "tracer_trace_adjoint",
 ]
 NOALLOC_MAX_PIXELS = 16384
 NOALLOC_MAX_ROUNDS = 8192
@@ -114,6 +114,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_upload_scenes.argtypes = [vp, ctypes.POINTER(SceneDesc), u32]
     lib.tracer_trace_batched.argtypes = [vp, vp, ctypes.POINTER(TraceParams), u32, i32, vp]
     lib.tracer_readback_scene.argtypes = [vp, u32, i32, vp, sz]
+    lib.tracer_trace_adjoint.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp, vp, vp, vp, vp, vp]
     if path is None:
         _lib = lib
     return lib
@@ -286,6 +287,8 @@ class Tracer:
             shape, dt = (h, w, 2), np.uint32
         elif aov == AOV_STATS:
             shape, dt = (len(STATS_FIELDS),), np.uint64
+        elif aov == AOV_LINEAR:
+            shape, dt = (h, w, 4), np.float32
         else:
             raise ValueError(aov)
         if out is None:
@@ -296,6 +299,42 @@ class Tracer:
     def stats(self) -> dict:
         v = self.readback(AOV_STATS)
         return {k: int(x) for k, x in zip(STATS_FIELDS, v)}
+
+    def trace_adjoint(self, frame: np.ndarray, params: TraceParams, dl_dimage, linear=None, num_materials=None,
+                      outputs=None, stream: int | None = None):
+        """tracer_trace_adjoint.  dl_dimage / linear: (h, w, 4) float32 numpy
+        arrays (host) or device addresses (ints).  Returns host arrays
+        (albedo (nm, 3), emission (nm, 3), campos (3,)), or, with outputs =
+        (albedo_ptr, emission_ptr, campos_ptr) device addresses, writes there
+        asynchronously and returns None."""
+        f = np.ascontiguousarray(np.asarray(frame, S.FRAME).reshape(()))
+
+        def ptr(x):
+            if x is None:
+                return None
+            if isinstance(x, int):
+                return ctypes.c_void_p(x)
+            return np.ascontiguousarray(x, np.float32).ctypes.data_as(ctypes.c_void_p)
+
+        keep = [np.ascontiguousarray(x, np.float32) for x in (dl_dimage, linear) if isinstance(x, np.ndarray)]
+        dl = keep[0].ctypes.data_as(ctypes.c_void_p) if isinstance(dl_dimage, np.ndarray) else ptr(dl_dimage)
+        ln = None
+        if linear is not None:
+            ln = keep[-1].ctypes.data_as(ctypes.c_void_p) if isinstance(linear, np.ndarray) else ptr(linear)
+        st = ctypes.c_void_p(stream) if stream else None
+        if outputs is not None:
+            self._check(self.lib.tracer_trace_adjoint(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
+                                                      dl, ln, ptr(outputs[0]), ptr(outputs[1]), ptr(outputs[2]), st))
+            return None
+        nm = num_materials
+        ga = np.zeros((nm, 3), np.float32)
+        ge = np.zeros((nm, 3), np.float32)
+        gc = np.zeros(3, np.float32)
+        self._check(self.lib.tracer_trace_adjoint(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params), dl,
+                                                  ln, ga.ctypes.data_as(ctypes.c_void_p),
+                                                  ge.ctypes.data_as(ctypes.c_void_p),
+                                                  gc.ctypes.data_as(ctypes.c_void_p), st))
+        return ga, ge, gc
 
     def set_profiling(self, on: bool):
         self._check(self.lib.tracer_set_profiling(self.h, 1 if on else 0))
