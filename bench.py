@@ -211,6 +211,191 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
                        "l2": "flushed before each timed step (256 MiB write)"}}
 
 
+def _perturbed_albedo(mats, seed, sigma=0.1):
+    from vktrace import scene as S
+    import numpy as np
+    g = S.SplitMix64(seed)
+    out = mats.copy()
+    out["albedo"] = np.clip(mats["albedo"] + sigma * g.normal(3 * len(mats)).reshape(-1, 3), 0.0, 1.0)
+    return out
+
+
+def adjoint_section(local: int, steps: int) -> dict:
+    """c3: 256^2, 4 spp, depth 4, 10k triangles in [-10,10]^3, 64 materials.
+    Target rendered with albedos perturbed by N(0, 0.1^2) (clamped); L2 image
+    loss.  Forward (wavefront) and adjoint (path replay) Mrays/s, device-timed
+    with every buffer resident; gradient spot check against central
+    differences of the forward (step 1e-3) on the largest albedo components."""
+    import numpy as np
+    import torch
+    from vktrace import abi, configs
+    wl = configs.c3()
+    tr = abi.Tracer(local)
+    tr.upload_scene(wl.scene)
+    base = wl.scene.materials.copy()
+    nm = len(base)
+    p = abi.Tracer.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                          sky=wl.sky, aovs=(abi.AOV_RGBA32F, abi.AOV_LINEAR), stats=True)
+    tr.set_materials(_perturbed_albedo(base, 3))
+    tr.trace(wl.frame, p)
+    target = tr.readback(abi.AOV_RGBA32F)
+    tr.set_materials(base)
+
+    def loss_dl(img):
+        d = img[:, 1:, :3].astype(np.float64) - target[:, 1:, :3]
+        dl = np.zeros(img.shape, np.float32)
+        dl[:, 1:, :3] = 2 * d
+        return float((d * d).sum()), dl
+
+    tr.trace(wl.frame, p)
+    fwd_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+    img = tr.readback(abi.AOV_RGBA32F)
+    lin = tr.readback(abi.AOV_LINEAR)
+    L0, dl = loss_dl(img)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    dl_d = torch.from_numpy(dl).cuda()
+    lin_d = torch.from_numpy(lin).cuda()
+    ga = torch.zeros((nm, 3), device="cuda")
+    ge = torch.zeros((nm, 3), device="cuda")
+    gc = torch.zeros(3, device="cuda")
+    p_run = abi.Tracer.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                              sky=wl.sky, aovs=(abi.AOV_RGBA32F, abi.AOV_LINEAR))
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        tr.synchronize()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        tr.synchronize()
+        return a.elapsed_time(b) / steps
+
+    ms_fwd = timed(lambda: tr.trace(wl.frame, p_run, sptr))
+    adj = lambda: tr.trace_adjoint(wl.frame, p_run, dl_d.data_ptr(), lin_d.data_ptr(),
+                                   outputs=(ga.data_ptr(), ge.data_ptr(), gc.data_ptr()), stream=sptr)
+    ms_adj = timed(adj)
+    adj_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+    g_alb = ga.cpu().numpy().astype(np.float64)
+    # spot check: central differences, step 1e-3, on the 6 largest components
+    idx = np.argsort(-np.abs(g_alb).ravel())[:6]
+    rel = []
+    for flat in idx:
+        m, c = divmod(int(flat), 3)
+        mp, mm = base.copy(), base.copy()
+        mp["albedo"][m, c] += 1e-3
+        mm["albedo"][m, c] -= 1e-3
+        tr.set_materials(mp)
+        tr.trace(wl.frame, p_run)
+        Lp, _ = loss_dl(tr.readback(abi.AOV_RGBA32F))
+        tr.set_materials(mm)
+        tr.trace(wl.frame, p_run)
+        Lm, _ = loss_dl(tr.readback(abi.AOV_RGBA32F))
+        fd = (Lp - Lm) / float(np.float32(mp["albedo"][m, c]) - np.float32(mm["albedo"][m, c]))
+        rel.append(abs(g_alb[m, c] - fd) / abs(fd))
+    tr.set_materials(base)
+    tr.close()
+    fwd = fwd_rays / (ms_fwd / 1e3) / 1e6
+    adjv = adj_rays / (ms_adj / 1e3) / 1e6
+    return {"metric": "adjoint Mrays/s (c3, path replay)", "value": adjv, "unit": UNIT, "ms_per_step": ms_adj,
+            "forward": {"value": fwd, "ms_per_step": ms_fwd, "rays_per_step": fwd_rays},
+            "adjoint_rays_per_step": adj_rays, "ratio_adjoint_to_forward": adjv / fwd,
+            "forward_rays_per_adjoint_second_ratio": ms_fwd / ms_adj,
+            "grad_check": {"max_rel_err_vs_central_fd": max(rel), "components": len(rel), "step": 1e-3},
+            "loss": L0,
+            "config": {"workload": wl.name, "triangles": len(wl.scene.triangles), "materials": nm}}
+
+
+def gd_section(local: int, gd_steps: int, width: int, spp: int, n_tris: int) -> dict:
+    """c4: recover perturbed albedos by gradient descent on an L2 image loss
+    (1024^2, 64 spp, depth 12, 1M triangles, 1024 materials by default).
+    Each step: forward (wavefront, RGBA32F + LINEAR) and adjoint, device-timed;
+    Adam on the albedo table, clamped to [1e-3, 1]."""
+    import numpy as np
+    import torch
+    from vktrace import abi, configs
+    wl = configs.c4(width=width, spp=spp, n_tris=n_tris)
+    tr = abi.Tracer(local)
+    tr.upload_scene(wl.scene)
+    truth = wl.scene.materials.copy()
+    nm = len(truth)
+    p = abi.Tracer.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                          sky=wl.sky, aovs=(abi.AOV_RGBA32F, abi.AOV_LINEAR), stats=True)
+    tr.trace(wl.frame, p)
+    target = torch.from_numpy(tr.readback(abi.AOV_RGBA32F)).cuda()
+    start = _perturbed_albedo(truth, 4)
+    alb = torch.tensor(start["albedo"], dtype=torch.float32, requires_grad=False)
+    opt_param = torch.nn.Parameter(alb.clone())
+    opt = torch.optim.Adam([opt_param], lr=0.01)
+    ga = torch.zeros((nm, 3), device="cuda")
+    ge = torch.zeros((nm, 3), device="cuda")
+    gc = torch.zeros(3, device="cuda")
+    free0, _ = torch.cuda.mem_get_info()
+    # a dedicated stream: the events must be recorded on the stream the tracer
+    # launches on (handle 0 would select the tracer's own stream instead)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    fwd_rates, adj_rates = [], []
+    mats = truth.copy()
+    seen = None
+    npx = wl.width * wl.height
+    peak_extra = 0
+    for step in range(gd_steps):
+        mats["albedo"] = opt_param.detach().numpy()
+        tr.set_materials(mats)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        tr.trace(wl.frame, p, sptr)
+        e1.record(stream)
+        tr.synchronize()
+        f_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+        ptr, _ = tr.device_image(abi.AOV_RGBA32F)
+        img = torch.empty((wl.height, wl.width, 4), device="cuda")
+        lin = torch.empty((wl.height, wl.width, 4), device="cuda")
+        torch.cuda.synchronize()
+        from vktrace.autograd import _DeviceView
+        img.copy_(torch.as_tensor(_DeviceView(ptr, img.shape, "<f4"), device="cuda"))
+        lptr, _ = tr.device_image(abi.AOV_LINEAR)
+        lin.copy_(torch.as_tensor(_DeviceView(lptr, lin.shape, "<f4"), device="cuda"))
+        dl = torch.zeros_like(img)
+        dl[:, 1:, :3] = 2.0 * (img[:, 1:, :3] - target[:, 1:, :3]) / npx
+        torch.cuda.synchronize()
+        e1b = torch.cuda.Event(enable_timing=True)
+        e1b.record(stream)
+        tr.trace_adjoint(wl.frame, p, dl.data_ptr(), lin.data_ptr(),
+                         outputs=(ga.data_ptr(), ge.data_ptr(), gc.data_ptr()), stream=sptr)
+        e2.record(stream)
+        tr.synchronize()
+        torch.cuda.synchronize()
+        peak_extra = max(peak_extra, free0 - torch.cuda.mem_get_info()[0])
+        a_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+        fwd_rates.append(f_rays / (e0.elapsed_time(e1) / 1e3) / 1e6)
+        adj_rates.append(a_rays / (e1b.elapsed_time(e2) / 1e3) / 1e6)
+        g = ga.cpu()
+        seen = (g != 0).any(dim=1) if seen is None else seen | (g != 0).any(dim=1)
+        opt.zero_grad()
+        opt_param.grad = g.clone()
+        opt.step()
+        with torch.no_grad():
+            opt_param.clamp_(1e-3, 1.0)
+    tr.close()
+    err0 = np.abs(start["albedo"] - truth["albedo"])[seen.numpy()]
+    err1 = np.abs(opt_param.detach().numpy() - truth["albedo"])[seen.numpy()]
+    return {"metric": "gradient descent on albedos (c4 shape)", "steps": gd_steps,
+            "forward_mrays_s": {"median": float(np.median(fwd_rates)), "min": float(np.min(fwd_rates))},
+            "adjoint_mrays_s": {"median": float(np.median(adj_rates)), "min": float(np.min(adj_rates))},
+            "albedo_mae": {"initial": float(err0.mean()), "final": float(err1.mean()),
+                           "materials_with_gradient": int(seen.sum()), "materials": nm},
+            "peak_extra_device_memory_bytes": int(peak_extra),
+            "config": {"workload": wl.name, "optimizer": "Adam lr 0.01, albedo clamped to [1e-3, 1]"}}
+
+
 def run_reference(args):
     """CPU restatement of the reference shader (oracle port, same BVH), timed
     on the host cores.  Rank 0 alone works under torchrun."""
@@ -391,6 +576,8 @@ def run_ours(args):
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         if world == 1 and not args.no_batched:
             line["batched"] = batched_section(local, max(3, args.steps // 2), 2)
+        if world == 1 and not args.no_adjoint:
+            line["adjoint"] = adjoint_section(local, max(3, args.steps // 2))
         print(json.dumps(line), flush=True)
     tr.close()
     if world > 1:
@@ -408,6 +595,10 @@ def main():
     ap.add_argument("--wavefront", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched section")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")
+    ap.add_argument("--gd-steps", type=int, default=0,
+                    help="run only the gradient-descent workload (c4 shape) for this many steps")
+    ap.add_argument("--gd-tris", type=int, default=1_000_000)
     # smaller variants of the workload (profiling captures); defaults = c1
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
@@ -415,7 +606,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.gd_steps:
+        import torch
+        torch.cuda.set_device(dist_setup()[2])
+        w = args.width if args.width != 1920 else 1024
+        spp = args.spp if args.spp != 16 else 64
+        print(json.dumps(gd_section(dist_setup()[2], args.gd_steps, w, spp, args.gd_tris)), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

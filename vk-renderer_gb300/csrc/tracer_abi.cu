@@ -65,12 +65,14 @@ struct SceneBuffers {
 
 struct AdjBuffers {
     DevBuf<float4> dldi, lin;
-    DevBuf<float> grad;
+    DevBuf<double> grad;  // FP64 sums the kernel accumulates into
+    DevBuf<float> gradf;  // the same, rounded to float for the outputs
     void release()
     {
         dldi.release();
         lin.release();
         grad.release();
+        gradf.release();
     }
 };
 
@@ -1295,6 +1297,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     const size_t ng = 6 * (size_t)s.nm + 3;
     cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
     cudaError_t e = dalloc(ab.grad, ng);
+    if (e == cudaSuccess) e = dalloc(ab.gradf, ng);
     const float4* dldi = reinterpret_cast<const float4*>(dL_dimage);
     if (e == cudaSuccess && !is_device_ptr(dL_dimage)) {
         e = dalloc(ab.dldi, npx);
@@ -1307,7 +1310,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         if (e == cudaSuccess) e = cudaMemcpyAsync(ab.lin.p, linear_image, npx * 16, cudaMemcpyHostToDevice, st);
         lin = ab.lin.p;
     }
-    if (e == cudaSuccess) e = cudaMemsetAsync(ab.grad.p, 0, ng * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ab.grad.p, 0, ng * sizeof(double), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
     if (e != cudaSuccess) return cuda_fail(c, e, "adjoint set-up");
@@ -1337,13 +1340,14 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     c->last_kernel = 3;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
-    c->last_launches = 1;
+    c->last_launches = 2;  // adjoint + FP64-to-float conversion
     c->last_mask = 1u << TRACER_AOV_STATS;
     c->width = p->width;
     c->height = p->height;
     if (c->profiling) cudaEventRecord(c->prof_begin, st);
     e = launch_adjoint(a, dldi, lin, ab.grad.p, s.nm, p->tie_mode, s.bvh ? 1 : 0, st);
     if (c->profiling) cudaEventRecord(c->prof_end, st);
+    if (e == cudaSuccess) e = launch_grad_to_float(ab.grad.p, ab.gradf.p, (uint32_t)ng, st);
     if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
     if (e != cudaSuccess) return cuda_fail(c, e, "adjoint launch");
     c->pending = true;
@@ -1355,7 +1359,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     for (int k = 0; k < 3; ++k) {
         if (!outs[k]) continue;
         if (is_device_ptr(outs[k])) {
-            e = cudaMemcpyAsync(outs[k], ab.grad.p + offs[k], lens[k] * sizeof(float), cudaMemcpyDeviceToDevice, st);
+            e = cudaMemcpyAsync(outs[k], ab.gradf.p + offs[k], lens[k] * sizeof(float), cudaMemcpyDeviceToDevice, st);
             if (e != cudaSuccess) return cuda_fail(c, e, "gradient copy");
         } else {
             host_out = true;
@@ -1368,7 +1372,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         if (r != TRACER_OK) return r;
         for (int k = 0; k < 3; ++k)
             if (outs[k] && !is_device_ptr(outs[k])) {
-                e = cudaMemcpy(outs[k], ab.grad.p + offs[k], lens[k] * sizeof(float), cudaMemcpyDeviceToHost);
+                e = cudaMemcpy(outs[k], ab.gradf.p + offs[k], lens[k] * sizeof(float), cudaMemcpyDeviceToHost);
                 if (e != cudaSuccess) return cuda_fail(c, e, "gradient readback");
             }
     }

@@ -81,16 +81,19 @@ __device__ __forceinline__ V3 djitter(V3 d, V3 dd, float cphi, float sphi, float
 struct AdjArgs {
     const float4* dldi;    // dL/dI per pixel (RGBA layout, alpha ignored)
     const float4* linear;  // accum / spp per pixel from the forward trace, or NULL (recomputed)
-    float* grad;           // [nm x 3 albedo][nm x 3 emission][3 camera position]
+    double* grad;          // [nm x 3 albedo][nm x 3 emission][3 camera position], FP64 sums
     uint32_t nm;
     int smem_grad;         // reduce in shared memory first
 };
 
 __device__ __forceinline__ bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
 
-__device__ __forceinline__ void gadd(float* g, int i, float v)
+// Gradient components are sums of many per-pixel terms of both signs (dL/dI
+// changes sign across the image), so they are accumulated in FP64: float sums
+// would lose relative precision to the cancellation.
+__device__ __forceinline__ void gadd(double* g, int i, float v)
 {
-    if (v != 0.0f && isfinite(v)) atomicAdd(g + i, v);
+    if (v != 0.0f && isfinite(v)) atomicAdd(g + i, (double)v);
 }
 
 // One emitter's next-event estimate (same operations as nee_one) with its
@@ -220,16 +223,17 @@ __global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
     const int tid = threadIdx.x, nthreads = blockDim.x;
     const Stack stk{smem + tid, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * nthreads) + tid, nthreads,
                     (int)a.stack_depth};
-    float* sgrad = reinterpret_cast<float*>(smem + 2 * (size_t)a.stack_depth * nthreads);
+    // gradient sums after the stack, 8-byte aligned
+    double* sgrad = reinterpret_cast<double*>(smem + 2 * (size_t)a.stack_depth * nthreads);
     const uint32_t ngrad = 6 * ga.nm + 3;
     if (ga.smem_grad) {
-        for (uint32_t k = tid; k < ngrad; k += nthreads) sgrad[k] = 0.0f;
+        for (uint32_t k = tid; k < ngrad; k += nthreads) sgrad[k] = 0.0;
         __syncthreads();
     }
-    float* grad = ga.smem_grad ? sgrad : ga.grad;
-    float* gal = grad;
-    float* gem = grad + 3 * ga.nm;
-    float* gcam = grad + 6 * ga.nm;
+    double* grad = ga.smem_grad ? sgrad : ga.grad;
+    double* gal = grad;
+    double* gem = grad + 3 * ga.nm;
+    double* gcam = grad + 6 * ga.nm;
     Counters cnt;
 #pragma unroll
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
     if (ga.smem_grad) {
         __syncthreads();
         for (uint32_t k = tid; k < ngrad; k += nthreads)
-            if (sgrad[k] != 0.0f) atomicAdd(ga.grad + k, sgrad[k]);
+            if (sgrad[k] != 0.0) atomicAdd(ga.grad + k, sgrad[k]);
     }
 }
 
@@ -412,7 +416,7 @@ template <int TIE, bool BVH, bool CAM>
 static cudaError_t adj_t(const TraceArgs& a, const AdjArgs& g, cudaStream_t s)
 {
     const uint32_t block = 128;
-    const size_t smem = (size_t)a.stack_depth * block * 8 + (g.smem_grad ? (6 * (size_t)g.nm + 3) * 4 : 0);
+    const size_t smem = (size_t)a.stack_depth * block * 8 + (g.smem_grad ? (6 * (size_t)g.nm + 3) * 8 : 0);
     auto k = k_adjoint<TIE, BVH, CAM>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((a.width + 15) / 16, (a.height + (block / 16) - 1) / (block / 16));
@@ -420,10 +424,23 @@ static cudaError_t adj_t(const TraceArgs& a, const AdjArgs& g, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, float* grad, uint32_t nm,
+__global__ void k_grad_to_float(const double* __restrict__ g, float* __restrict__ out, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)g[i];
+}
+
+cudaError_t launch_grad_to_float(const double* g, float* out, uint32_t n, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+    k_grad_to_float<<<blocks, 256, 0, s>>>(g, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, double* grad, uint32_t nm,
                            int tie, int bvh, cudaStream_t s)
 {
-    AdjArgs g{dldi, linear, grad, nm, (6 * (size_t)nm + 3) * 4 <= 96 * 1024 ? 1 : 0};
+    AdjArgs g{dldi, linear, grad, nm, (6 * (size_t)nm + 3) * 8 <= 96 * 1024 ? 1 : 0};
     const bool cam = a.sc.ne > 0;
     if (tie == TIE_REFERENCE) return cam ? adj_t<TIE_REFERENCE, false, true>(a, g, s) : adj_t<TIE_REFERENCE, false, false>(a, g, s);
     if (bvh) return cam ? adj_t<TIE_STRICT, true, true>(a, g, s) : adj_t<TIE_STRICT, true, false>(a, g, s);

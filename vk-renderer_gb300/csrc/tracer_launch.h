@@ -19,7 +19,9 @@ struct LaunchConfig {
 };
 
 cudaError_t launch_plain(const TraceArgs& a, const LaunchConfig& lc, cudaStream_t s);
-cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, float* grad, uint32_t nm,
+cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, double* grad, uint32_t nm,
                            int tie, int bvh, cudaStream_t s);
+// out[i] = (float)g[i], i < n
+cudaError_t launch_grad_to_float(const double* g, float* out, uint32_t n, cudaStream_t s);
 
 }  // namespace vkt
