@@ -279,25 +279,43 @@ def adjoint_section(local: int, steps: int) -> dict:
     ms_fwd = timed(lambda: tr.trace(wl.frame, p_run, sptr))
     adj = lambda: tr.trace_adjoint(wl.frame, p_run, dl_d.data_ptr(), lin_d.data_ptr(),
                                    outputs=(ga.data_ptr(), ge.data_ptr(), gc.data_ptr()), stream=sptr)
-    ms_adj = timed(adj)
+    ms_adj = timed(adj)  # AUTO: the per-pixel kernel below 2^17 pixels, else the wavefront
     adj_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+    # both adjoint forms on the same inputs, for comparison
+    per_kernel = {}
+    for name, k in (("per_pixel", abi.KERNEL_PLAIN), ("wavefront", abi.KERNEL_WAVEFRONT)):
+        p_run.kernel = k
+        ms_k = timed(adj)
+        per_kernel[name] = {"value": adj_rays / (ms_k / 1e3) / 1e6, "ms_per_step": ms_k}
+    p_run.kernel = abi.KERNEL_AUTO
     g_alb = ga.cpu().numpy().astype(np.float64)
-    # spot check: central differences, step 1e-3, on the 6 largest components
+    # spot check: central differences, step 1e-3, on the 6 largest components.
+    # A 1e-3 step is up to 10 % of a small albedo, where the loss's curvature
+    # makes that difference itself off by ~1e-3 relative; the Richardson
+    # combination of steps 1e-3 and 5e-4, (4 fd(h/2) - fd(h)) / 3, cancels
+    # that h^2 term.
     idx = np.argsort(-np.abs(g_alb).ravel())[:6]
-    rel = []
-    for flat in idx:
-        m, c = divmod(int(flat), 3)
+
+    def central(m, c, h):
         mp, mm = base.copy(), base.copy()
-        mp["albedo"][m, c] += 1e-3
-        mm["albedo"][m, c] -= 1e-3
+        mp["albedo"][m, c] += h
+        mm["albedo"][m, c] -= h
         tr.set_materials(mp)
         tr.trace(wl.frame, p_run)
         Lp, _ = loss_dl(tr.readback(abi.AOV_RGBA32F))
         tr.set_materials(mm)
         tr.trace(wl.frame, p_run)
         Lm, _ = loss_dl(tr.readback(abi.AOV_RGBA32F))
-        fd = (Lp - Lm) / float(np.float32(mp["albedo"][m, c]) - np.float32(mm["albedo"][m, c]))
-        rel.append(abs(g_alb[m, c] - fd) / abs(fd))
+        return (Lp - Lm) / float(np.float32(mp["albedo"][m, c]) - np.float32(mm["albedo"][m, c]))
+
+    rel, rel_r = [], []
+    for flat in idx:
+        m, c = divmod(int(flat), 3)
+        f1 = central(m, c, 1e-3)
+        f2 = central(m, c, 5e-4)
+        fr = (4.0 * f2 - f1) / 3.0
+        rel.append(abs(g_alb[m, c] - f1) / abs(f1))
+        rel_r.append(abs(g_alb[m, c] - fr) / abs(fr))
     tr.set_materials(base)
     tr.close()
     fwd = fwd_rays / (ms_fwd / 1e3) / 1e6
@@ -305,8 +323,12 @@ def adjoint_section(local: int, steps: int) -> dict:
     return {"metric": "adjoint Mrays/s (c3, path replay)", "value": adjv, "unit": UNIT, "ms_per_step": ms_adj,
             "forward": {"value": fwd, "ms_per_step": ms_fwd, "rays_per_step": fwd_rays},
             "adjoint_rays_per_step": adj_rays, "ratio_adjoint_to_forward": adjv / fwd,
+            "kernel": "auto (" + ("wavefront" if wl.width * wl.height >= 1 << 17 else "per-pixel") + ")",
+            "kernels": per_kernel,
             "forward_rays_per_adjoint_second_ratio": ms_fwd / ms_adj,
-            "grad_check": {"max_rel_err_vs_central_fd": max(rel), "components": len(rel), "step": 1e-3},
+            "grad_check": {"max_rel_err_vs_central_fd": max(rel), "step": 1e-3,
+                           "max_rel_err_vs_richardson_fd": max(rel_r), "steps": [1e-3, 5e-4],
+                           "components": len(rel)},
             "loss": L0,
             "config": {"workload": wl.name, "triangles": len(wl.scene.triangles), "materials": nm}}
 
@@ -460,7 +482,7 @@ def run_ours(args):
     sptr = stream.cuda_stream
     kern = abi.KERNEL_WAVEFRONT if args.kernel == "wavefront" else abi.KERNEL_PLAIN
     common = dict(spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start, sky=wl.sky, kernel=kern,
-                  block=args.block, wavefront=args.wavefront)
+                  block=args.block, wavefront=args.wavefront, bvh_width=args.bvh_width)
     p_run = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=False, **common)
     # counting pass (untimed) with the plain kernel, whose node-visiting order
     # is the oracle's: the canonical ray / node / primitive counts of the frame.
@@ -552,6 +574,8 @@ def run_ours(args):
                        "max_depth": wl.max_depth, "rr_start": wl.rr_start,
                        "triangles": len(wl.scene.triangles), "materials": len(wl.scene.materials),
                        "bvh": f"sah16-leaf4 depth {bvh_depth}", "kernel": args.kernel, "block": args.block,
+                       "traversal": {0: "auto (4-wide when the stack allows)", 2: "binary",
+                                     4: "4-wide"}[args.bvh_width],
                        "l2": "flushed before each timed step (256 MiB write)",
                        "parallelism": f"replica per GPU x{world} (independent frames)"},
             "rays_per_step": rays,
@@ -593,6 +617,8 @@ def main():
     ap.add_argument("--kernel", choices=["wavefront", "plain"], default="wavefront")
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--wavefront", type=int, default=0)
+    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4],
+                    help="wavefront traversal: 0 auto (4-wide), 2 binary, 4 4-wide")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched section")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")

@@ -199,6 +199,8 @@ typedef struct tracer_trace_params {
     uint32_t wavefront;     /* wavefront extend kernel: resident CTAs per SM; 0 = occupancy maximum */
     uint32_t aov_mask;      /* bit (1 << TRACER_AOV_*) per image written; 0 = RGBA8 only */
     uint32_t stats;         /* nonzero: count rays, node fetches and primitive tests */
+    uint32_t bvh_width;     /* wavefront traversal: 0 = auto (4-wide nodes when the stack allows), 2 = the
+                               binary BVH, 4 = 4-wide nodes collapsed from it (same boxes, same hits) */
 } tracer_trace_params;
 
 typedef struct tracer_stats {
@@ -333,6 +335,114 @@ int tracer_last_timings(tracer_ctx* ctx, tracer_timings* out);
 #define TRACER_NOALLOC_MAX_ROUNDS 8192u  /* spp * max_depth */
 int tracer_trace_noalloc(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
                          void* rgba8_out, void* rgba32f_out, void* cuda_stream);
+
+/* ------------------------------------------------------------ present pass
+ * The step after the dispatch: the reference's fragment shader
+ * Assets/Fullscreen.frag, drawn over the window by a fullscreen triangle
+ * (Assets/Fullscreen.vert) in GraphicsDevice::Draw (Source/
+ * GraphicsDevice.cpp:1286-1308), here into a headless framebuffer.  Per
+ * output pixel: the traced image is sampled at the pixel's uv, flipped
+ * vertically (the traced image's row 0 is its bottom), with bilinear
+ * filtering and clamp-to-border black (GraphicsDevice.cpp:770-790); where the
+ * squared difference to the previous frame's image exceeds 0.0005 the
+ * output is the mean of four taps half a texel of a 1024^2 image away (1/2048
+ * in uv, Fullscreen.frag:12), else the centre tap.  The framebuffer's row 0
+ * is its top row; channels are in RGBA order (the reference's swapchain is
+ * B8G8R8A8_UNORM: the same bytes, swizzled). */
+typedef struct tracer_present_params {
+    uint32_t width, height; /* framebuffer extent (the reference's window, 1024 x 768, Main.cpp:92) */
+    uint32_t out_aov;       /* TRACER_AOV_RGBA8 (UNORM8) or TRACER_AOV_RGBA32F */
+    uint32_t mode;          /* tracer_draw: TRACER_PRESENT_PINGPONG or TRACER_PRESENT_ACCUMULATE */
+} tracer_present_params;
+
+/* Frame k is traced into image slot k % 2 and the present pass reads slot 0
+ * as the current image and slot 1 as the previous one, as the reference binds
+ * them (traced_images, Source/VulkanState.h:106-108, bound at
+ * GraphicsDevice.cpp:955-983; currentFrame alternates, :1341). */
+#define TRACER_PRESENT_PINGPONG 0u
+/* Progressive accumulation (no counterpart in the reference): the frames'
+ * linear radiance (LINEAR AOV) is summed on the device while the camera,
+ * aspect ratio, trace parameters and scene stay the same (any change, or
+ * tracer_draw_reset, restarts the sum); the present pass reads the
+ * tonemapped mean after this frame as the current image and the mean before
+ * it as the previous one, so its variance test sees the estimate converge.
+ * Pass a new frame seed per call for new samples. */
+#define TRACER_PRESENT_ACCUMULATE 1u
+
+/* The present pass alone over caller images: image0 is the image bound as
+ * raytraced_image, image1 as prev_raytraced_image; both src_width x
+ * src_height, TRACER_AOV_RGBA8 (4 bytes per texel) or TRACER_AOV_RGBA32F (16
+ * bytes), host or device memory.  out: width*height*4 bytes (RGBA8) or *16
+ * (RGBA32F), host (the call waits, bounded) or device (asynchronous on
+ * cuda_stream).  pp->mode is ignored. */
+int tracer_present(tracer_ctx* ctx, const void* image0, const void* image1, uint32_t src_width, uint32_t src_height,
+                   int src_aov, const tracer_present_params* pp, void* out, size_t out_bytes, void* cuda_stream);
+
+/* One GraphicsDevice::Draw (GraphicsDevice.cpp:1236-1343) without the window:
+ * tracer_trace of frame/params (RGBA8, plus LINEAR in ACCUMULATE mode, are
+ * added to params->aov_mask), then the present pass into out as for
+ * tracer_present.  The frame's seed and aspect ratio are used as given (the
+ * reference sets them per frame: rand() / RAND_MAX and the swapchain's
+ * aspect, GraphicsDevice.cpp:1258-1262). */
+int tracer_draw(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
+                const tracer_present_params* pp, void* out, size_t out_bytes, void* cuda_stream);
+
+/* Clears both frame slots (to black) and the accumulation; the next draw is
+ * frame 0. */
+int tracer_draw_reset(tracer_ctx* ctx);
+
+/* ------------------------------------------------------------ camera
+ * The reference's camera controller (Camera, Source/Camera.cpp:5-64) with the
+ * input handling of its main loop (Source/Main.cpp:23-83), for scripted
+ * camera paths: a sequence of per-frame inputs gives the FrameData camera of
+ * every frame.  Host only, single precision, no fused multiply-add. */
+typedef struct tracer_camera_controller {
+    tracer_camera data;   /* CameraData: pos, dir, right, up */
+    float front[3];       /* CameraDataAux::front */
+    float pitch, yaw;     /* degrees */
+    float last_mouse[2];  /* last cursor position seen (Main.cpp:17-18) */
+    uint32_t light_locked; /* light_pos follows the camera (Main.cpp:20, :178) */
+    float light_pos[3];   /* FrameData::light_pos: (0, 64, 0) at start (Main.cpp:141) */
+} tracer_camera_controller;
+
+#define TRACER_KEY_W 1u  /* move_forward  (Main.cpp:27-30) */
+#define TRACER_KEY_S 2u  /* move_backward, only without W */
+#define TRACER_KEY_A 4u  /* move_left */
+#define TRACER_KEY_D 8u  /* move_right, only without A */
+#define TRACER_KEY_R 16u /* move_up */
+#define TRACER_KEY_F 32u /* move_down, only without R */
+
+/* One frame of input, applied in the order of the main loop (Main.cpp:150-180):
+ * cursor events (mouse_callback) and the E key (key_callback) arrive while
+ * events are polled, then the held keys move the camera by 111 * dt. */
+typedef struct tracer_input_frame {
+    float dt;               /* seconds since the previous frame */
+    uint32_t keys;          /* TRACER_KEY_* held */
+    uint32_t toggle_light;  /* E pressed this frame */
+    uint32_t has_cursor;    /* a cursor event at (cursor_x, cursor_y) */
+    double cursor_x, cursor_y;
+} tracer_input_frame;
+
+/* Camera::Camera(): pos (0, 64, -48), pitch 0, yaw 90 (Camera.cpp:5-10). */
+void tracer_camera_init(tracer_camera_controller* cam);
+/* The start-up camera of the reference's main loop (Main.cpp:134-139). */
+void tracer_camera_init_startup(tracer_camera_controller* cam);
+/* Camera::update (Camera.cpp:48-64): pitch clamped to [-89, 89]; front from
+ * pitch and yaw; dir, right, up from front. */
+void tracer_camera_update(tracer_camera_controller* cam);
+/* Camera::move_forward .. move_down (Camera.cpp:12-46), direction 0..5 =
+ * forward, backward, left, right, up, down. */
+int tracer_camera_move(tracer_camera_controller* cam, int direction, float speed);
+/* mouse_callback (Main.cpp:66-83) for a cursor event at (x, y). */
+void tracer_camera_cursor(tracer_camera_controller* cam, double x, double y);
+/* poll_keyboard (Main.cpp:23-51). */
+void tracer_camera_keys(tracer_camera_controller* cam, uint32_t keys, float dt);
+/* Applies n frames of input; frames_out[i] (may be NULL) receives the frame's
+ * FrameData camera and light_pos (which follows the camera position +
+ * (0, -1, 0) while the light is locked and stays put otherwise, Main.cpp:
+ * 176-178); aspect_ratio and seed are left as they were in frames_out[i]. */
+int tracer_camera_script(tracer_camera_controller* cam, const tracer_input_frame* inputs, uint32_t n,
+                         tracer_frame* frames_out);
 
 #ifdef __cplusplus
 }

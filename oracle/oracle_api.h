@@ -56,6 +56,25 @@ int oracle_trace_ray(const oracle_scene* scene, int tie_mode, int shadow, const 
 void oracle_radiance(const oracle_scene* scene, const float* frame96, const oracle_params* params, const float* o,
                      const float* d, float cx, float cy, float salt, float* out_rgb, float* out_salt);
 
+/* present_oracle.cpp: the present pass (Fullscreen.frag), progressive
+ * accumulation and the camera controller (Camera.cpp, Main.cpp input). */
+void oracle_present(const void* image0, const void* image1, int src_is_float, uint32_t src_w, uint32_t src_h,
+                    uint32_t width, uint32_t height, float* out_rgba32f, uint8_t* out_rgba8);
+void oracle_accumulate(const float* linear_rgba, float* sum_rgba, uint32_t n_pixels, uint32_t n,
+                       float* display_rgba);
+
+typedef struct oracle_camera_ctl {
+    float cam[16];        /* CameraData: pos, dir, right, up (16-byte lanes) */
+    float front[3];
+    float pitch, yaw;     /* degrees */
+    float last_mouse[2];
+} oracle_camera_ctl;
+void oracle_camera_init(oracle_camera_ctl* c);
+void oracle_camera_update(oracle_camera_ctl* c);
+void oracle_camera_move(oracle_camera_ctl* c, int dir, float speed);
+void oracle_camera_mouse(oracle_camera_ctl* c, double x, double y);
+void oracle_camera_keyboard(oracle_camera_ctl* c, uint32_t keys, float dt);
+
 #ifdef __cplusplus
 }
 #endif

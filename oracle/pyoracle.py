@@ -40,6 +40,11 @@ class OStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in STATS_FIELDS]
 
 
+class OCameraCtl(ctypes.Structure):
+    _fields_ = [("cam", ctypes.c_float * 16), ("front", ctypes.c_float * 3), ("pitch", ctypes.c_float),
+                ("yaw", ctypes.c_float), ("last_mouse", ctypes.c_float * 2)]
+
+
 def build() -> str:
     """Builds liboracle.so (make -C oracle)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -85,6 +90,18 @@ def lib() -> ctypes.CDLL:
         L.oracle_radiance.argtypes = [ctypes.POINTER(OScene), vp, ctypes.POINTER(OParams), vp, vp, f32, f32, f32,
                                       vp, vp]
         L.oracle_radiance.restype = None
+        u32 = ctypes.c_uint32
+        L.oracle_present.argtypes = [vp, vp, i32, u32, u32, u32, u32, vp, vp]
+        L.oracle_present.restype = None
+        L.oracle_accumulate.argtypes = [vp, vp, u32, u32, vp]
+        L.oracle_accumulate.restype = None
+        pc = ctypes.POINTER(OCameraCtl)
+        for fn, args in (("oracle_camera_init", [pc]), ("oracle_camera_update", [pc]),
+                         ("oracle_camera_move", [pc, i32, f32]),
+                         ("oracle_camera_mouse", [pc, ctypes.c_double, ctypes.c_double]),
+                         ("oracle_camera_keyboard", [pc, u32, f32])):
+            getattr(L, fn).argtypes = args
+            getattr(L, fn).restype = None
         _lib = L
     return _lib
 
@@ -248,4 +265,79 @@ def ref_camera(pos, pitch, yaw):
     L.ref_camera.argtypes = [f32, f32, f32, f32, f32, ctypes.c_void_p]
     L.ref_camera.restype = None
     L.ref_camera(pos[0], pos[1], pos[2], pitch, yaw, _p(out))
+    return out
+
+
+# ------------------------------------------------ present / accumulate --
+def present(image0, image1, width, height):
+    """The present pass (Fullscreen.frag) over two (h, w, 4) source images,
+    uint8 (RGBA8 UNORM) or float32; returns (rgba32f, rgba8) of the
+    width x height framebuffer, row 0 at the top."""
+    a = np.ascontiguousarray(image0)
+    b = np.ascontiguousarray(image1)
+    assert a.shape == b.shape and a.dtype == b.dtype and a.dtype in (np.uint8, np.float32)
+    out32 = np.zeros((height, width, 4), np.float32)
+    out8 = np.zeros((height, width, 4), np.uint8)
+    lib().oracle_present(_p(a), _p(b), int(a.dtype == np.float32), a.shape[1], a.shape[0], width, height,
+                         _p(out32), _p(out8))
+    return out32, out8
+
+
+def accumulate(linear, sum_rgba, n):
+    """One frame of progressive accumulation: sum_rgba (h, w, 4) float32 is
+    updated in place; returns the tonemapped mean after n frames."""
+    lin = np.ascontiguousarray(linear, np.float32)
+    assert sum_rgba.flags.c_contiguous and sum_rgba.dtype == np.float32
+    disp = np.zeros_like(lin)
+    lib().oracle_accumulate(_p(lin), _p(sum_rgba), lin.shape[0] * lin.shape[1], n, _p(disp))
+    return disp
+
+
+class CameraCtl:
+    """The camera controller restated (Camera.cpp, Main.cpp input)."""
+
+    def __init__(self):
+        self.c = OCameraCtl()
+        lib().oracle_camera_init(ctypes.byref(self.c))
+
+    def update(self):
+        lib().oracle_camera_update(ctypes.byref(self.c))
+
+    def move(self, direction, speed):
+        lib().oracle_camera_move(ctypes.byref(self.c), direction, speed)
+
+    def mouse(self, x, y):
+        lib().oracle_camera_mouse(ctypes.byref(self.c), x, y)
+
+    def keyboard(self, keys, dt):
+        lib().oracle_camera_keyboard(ctypes.byref(self.c), keys, dt)
+
+    def state(self) -> np.ndarray:
+        """CameraData (16), front (3), pitch, yaw as float32 (21)."""
+        c = self.c
+        return np.array(list(c.cam) + list(c.front) + [c.pitch, c.yaw], np.float32)
+
+
+def ref_present(image0, image1, width, height):
+    """The reference's Fullscreen.frag compiled for the host (oracle/_ref)."""
+    L = ctypes.CDLL(os.path.join(REF_DIR, "libref_present.so"))
+    u32 = ctypes.c_uint32
+    L.ref_present.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, u32, u32, u32, u32, ctypes.c_void_p]
+    L.ref_present.restype = None
+    a = np.ascontiguousarray(image0)
+    b = np.ascontiguousarray(image1)
+    out = np.zeros((height, width, 4), np.float32)
+    L.ref_present(_p(a), _p(b), int(a.dtype == np.float32), a.shape[1], a.shape[0], width, height, _p(out))
+    return out
+
+
+def ref_camera_ops(ops, args):
+    """Camera.cpp operations from the default camera; (n, 21) states."""
+    L = ctypes.CDLL(os.path.join(REF_DIR, "libref_camera.so"))
+    L.ref_camera_ops.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.ref_camera_ops.restype = None
+    op = np.ascontiguousarray(ops, np.int32)
+    ar = np.ascontiguousarray(args, np.float32).reshape(-1)
+    out = np.zeros((len(op), 21), np.float32)
+    L.ref_camera_ops(len(op), _p(op), _p(ar), _p(out))
     return out

@@ -16,7 +16,12 @@ those libraries and records their outputs:
   kat_intersect.npz  calc_tri/sphere/plane_intersect on random rays
   kat_trace.npz      trace_ray on random rays through the Ref scene + triangles
 
+  ref_present.npz    the present pass (Assets/Fullscreen.frag) on random image
+                     pairs, RGBA8 and float
+  ref_camera.npz     Camera.cpp operations from the default camera
+
 Run here (needs the reference tree):  python tests/golden/make_golden.py
+(--present: only the last two)
 """
 from __future__ import annotations
 
@@ -56,9 +61,53 @@ def random_tris(seed: int, n: int) -> np.ndarray:
     return t
 
 
+def present_and_camera():
+    """ref_present.npz: Fullscreen.frag compiled for the host over random
+    image pairs (RGBA8 and float, equal and differing regions, the Ref sizes
+    1024^2 -> 1024x768 and ragged ones).  ref_camera.npz: Camera.cpp
+    operations from the default camera (moves, pitch/yaw changes past the
+    +-89 clamp, the start-up camera)."""
+    g = np.random.default_rng(20240)
+    pres = {}
+    cases = [(64, 64, 48, 40), (37, 23, 50, 71), (1, 1, 3, 2), (1024, 1024, 1024, 768)]
+    for k, (sw, sh, w, h) in enumerate(cases):
+        a8 = g.integers(0, 256, (sh, sw, 4), dtype=np.uint8)
+        b8 = a8.copy()
+        noisy = g.random((sh, sw)) < 0.5  # half the texels differ from the previous frame
+        b8[noisy] = g.integers(0, 256, (int(noisy.sum()), 4), dtype=np.uint8)
+        af = g.random((sh, sw, 4), dtype=np.float32)
+        bf = af + np.where(g.random((sh, sw, 1)) < 0.5, np.float32(0.05), np.float32(0.0)).astype(np.float32)
+        out8 = pyoracle.ref_present(a8, b8, w, h)
+        outf = pyoracle.ref_present(af, bf, w, h)
+        if sw * sh > 4096:  # large case: seeds regenerate the inputs; store hashes and crops
+            pres[f"c{k}_seed_note"] = np.array("inputs regenerated by the test from the same generator")
+            pres[f"c{k}_u8_sha"] = np.array(sha(out8))
+            pres[f"c{k}_f32_sha"] = np.array(sha(outf))
+            pres[f"c{k}_u8_crop"] = out8[300:332, 500:532]
+            pres[f"c{k}_f32_crop"] = outf[300:332, 500:532]
+        else:
+            pres[f"c{k}_a8"], pres[f"c{k}_b8"], pres[f"c{k}_af"], pres[f"c{k}_bf"] = a8, b8, af, bf
+            pres[f"c{k}_u8"], pres[f"c{k}_f32"] = out8, outf
+    pres["cases"] = np.array(cases, np.int32)
+    pres["rng_seed"] = np.int64(20240)
+    np.savez_compressed(os.path.join(HERE, "ref_present.npz"), **pres)
+
+    ops = [0, 2, 6, 6, 4, 1, 3, 5, 6, 6, 7, 0, 6, 2]
+    args = [3.5, 0, 2.25, 0, 10.5, -3.25, 0.0, 200.0, 1.5, 0, 0.75, 0, 5.0, 0, 2.0, 0, -7.0, -150.0,
+            33.3, 71.2, 0, 0, 1.1, 0, 4.2, -1.7, 0.6, 0]
+    states = pyoracle.ref_camera_ops(ops, args)
+    np.savez(os.path.join(HERE, "ref_camera.npz"), ops=np.array(ops, np.int32),
+             args=np.array(args, np.float32).reshape(-1, 2), states=states)
+
+
 def main():
     if not pyoracle.build_ref():
         raise SystemExit("reference tree not found")
+    if "--present" in sys.argv:
+        present_and_camera()
+        print("present and camera vectors written to", HERE)
+        return
+    present_and_camera()
     out = {}
     H = {False: pyoracle.RefHarness(False), True: pyoracle.RefHarness(True)}
     sph, pl, tm, (depth, samples) = H[False].scene_constants()

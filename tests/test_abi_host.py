@@ -34,6 +34,8 @@ int main(void) {
   S(tracer_bvh_node); P(tracer_bvh_node, bmin); P(tracer_bvh_node, left_or_first); P(tracer_bvh_node, bmax);
   P(tracer_bvh_node, count);
   S(tracer_stats); S(tracer_trace_params); S(tracer_scene_desc); S(tracer_timings);
+  S(tracer_present_params); S(tracer_camera_controller); S(tracer_input_frame);
+  P(tracer_camera_controller, front); P(tracer_camera_controller, light_pos); P(tracer_input_frame, cursor_x);
   return 0;
 }
 """
@@ -92,6 +94,12 @@ def test_numpy_dtypes_match_header(layout):
     assert ctypes.sizeof(abi.TraceParams) == layout["tracer_trace_params"]
     assert ctypes.sizeof(abi.SceneDesc) == layout["tracer_scene_desc"]
     assert ctypes.sizeof(abi.Timings) == layout["tracer_timings"]
+    assert ctypes.sizeof(abi.PresentParams) == layout["tracer_present_params"]
+    assert ctypes.sizeof(abi.CameraController) == layout["tracer_camera_controller"]
+    assert ctypes.sizeof(abi.InputFrame) == layout["tracer_input_frame"]
+    assert abi.CameraController.front.offset == layout["tracer_camera_controller.front"]
+    assert abi.CameraController.light_pos.offset == layout["tracer_camera_controller.light_pos"]
+    assert abi.InputFrame.cursor_x.offset == layout["tracer_input_frame.cursor_x"]
 
 
 def declared_functions():

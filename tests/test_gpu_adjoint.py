@@ -143,6 +143,46 @@ def test_adjoint_vs_fp64_host(gpu_tracer):
     _compare(ga, fd, "albedo vs FP64")
 
 
+@pytest.mark.parametrize("case", ["sah-rr0", "sah-rr3-ragged", "linear-reference-ties"])
+def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case):
+    """Scenes without emitters take the wavefront adjoint (both passes as
+    queue stages, closest hits through the forward extend kernel); the
+    per-pixel adjoint kernel runs the same passes.  Ray and hit counts are
+    equal; gradients are equal up to the order of the FP64 sums."""
+    tr = gpu_tracer
+    sc = _scene(seed=21, n=2000, nm=16)
+    tie = abi.TIES_STRICT
+    if case.startswith("linear"):
+        sc = S.Scene(triangles=sc.triangles[:300], materials=sc.materials, bvh=S.BVH_NONE)
+        tie = abi.TIES_REFERENCE
+    tr.upload_scene(sc)
+    w, h = (77, 53) if "ragged" in case else (64, 64)
+    rr = 0 if "rr0" in case or case.startswith("linear") else 3
+    fr = S.frame(S.look_at((2.0, 1.0, 25.0), (0.0, 0.0, 0.0), 40.0), w / h, 0.45)
+    p = abi.Tracer.params(w, h, spp=3, max_depth=5, rr_start=rr, sky=(1.0, 1.0, 1.0), tie_mode=tie,
+                          aovs=(abi.AOV_RGBA32F, abi.AOV_LINEAR), kernel=abi.KERNEL_WAVEFRONT)
+    base = sc.materials.copy()
+    tgt_m = base.copy()
+    tgt_m["albedo"] = np.clip(base["albedo"] * 0.7 + 0.2, 0, 1)
+    target, _ = _render(tr, sc, fr, p, tgt_m)
+    img, lin = _render(tr, sc, fr, p, base)
+    _, dl = _loss_and_dl(img, target)
+    out = {}
+    for k in (abi.KERNEL_PLAIN, abi.KERNEL_WAVEFRONT):
+        p.kernel = k
+        ga, ge, gc = tr.trace_adjoint(fr, p, dl, lin, num_materials=len(base))
+        out[k] = (ga, ge, gc, tr.stats())
+    pa, pe, pc, ps = out[abi.KERNEL_PLAIN]
+    wa, we, wc, ws = out[abi.KERNEL_WAVEFRONT]
+    assert ps["closest_rays"] == ws["closest_rays"] and ps["hits"] == ws["hits"]
+    assert ps["shadow_rays"] == ws["shadow_rays"] == 0
+    assert np.all(wc == 0.0) and np.all(pc == 0.0)
+    for a, b in ((pa, wa), (pe, we)):
+        scale = float(np.max(np.abs(a))) if np.any(a) else 1.0
+        np.testing.assert_allclose(b, a, rtol=1e-5, atol=1e-7 * scale)
+    assert np.any(wa != 0)
+
+
 def _nee_scene(kind):
     """Scenes whose depth-1 image depends smoothly on the camera position
     (through the hit points, the sphere normals and the next-event view

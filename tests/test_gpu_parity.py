@@ -80,6 +80,48 @@ def test_kernels_identical(gpu_tracer):
         assert a["stats"][k] == b["stats"][k]
 
 
+@pytest.mark.parametrize("prims", ["triangles", "spheres", "mixed"])
+def test_wide_traversal_identical(gpu_tracer, prims):
+    """The wavefront's 4-wide traversal (nodes collapsed from the binary BVH,
+    same boxes) gives the binary traversal's and the plain kernel's bits."""
+    ref = S.reference_scene()
+    if prims == "spheres":
+        sc = sphere_scene(3)
+    else:
+        sc = soup_scene(6, 4000, extent=12.0, sigma=0.5)
+        if prims == "mixed":
+            sc.spheres = ref.spheres  # one emitter: next-event shadow rays too
+    fr = S.frame(S.look_at((0.0, 3.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.2, 0.4)
+    out = {}
+    for name, kernel, width in (("plain", abi.KERNEL_PLAIN, 0), ("binary", abi.KERNEL_WAVEFRONT, 2),
+                                ("wide", abi.KERNEL_WAVEFRONT, 4)):
+        gpu_tracer.upload_scene(sc)
+        p = abi.Tracer.params(72, 60, spp=3, max_depth=5, rr_start=2, sky=(0.9, 0.95, 1.0), kernel=kernel,
+                              aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F, abi.AOV_PRIMARY_HIT), stats=True,
+                              bvh_width=width)
+        gpu_tracer.trace(fr, p)
+        out[name] = (gpu_tracer.readback(abi.AOV_RGBA32F), gpu_tracer.readback(abi.AOV_PRIMARY_HIT),
+                     gpu_tracer.stats())
+    for name in ("binary", "wide"):
+        assert np.array_equal(fbits(out[name][0]), fbits(out["plain"][0])), name
+        assert np.array_equal(out[name][1], out["plain"][1]), name
+        for k in ("closest_rays", "shadow_rays", "hits"):
+            assert out[name][2][k] == out["plain"][2][k], (name, k)
+
+
+def test_wide_traversal_stack_check(gpu_tracer):
+    sc = soup_scene(6, 4000, extent=12.0, sigma=0.5)
+    gpu_tracer.upload_scene(sc)
+    fr = S.frame(S.look_at((0.0, 3.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.4)
+    p = abi.Tracer.params(16, 16, spp=1, max_depth=2, kernel=abi.KERNEL_WAVEFRONT, stack_depth=4, bvh_width=4)
+    with pytest.raises(abi.TracerError) as e:
+        gpu_tracer.trace(fr, p)
+    assert e.value.status in (abi.ERR_STACK_OVERFLOW,)
+    p.bvh_width = 3
+    with pytest.raises(abi.TracerError):
+        gpu_tracer.trace(fr, p)
+
+
 def test_bvh_equals_linear_strict(gpu_tracer):
     """Strict ties make the result independent of traversal order: the BVH
     image equals the linear-scan image."""

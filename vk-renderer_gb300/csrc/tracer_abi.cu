@@ -24,6 +24,8 @@
 #include "tracer_abi.h"
 #include "tracer_core.cuh"
 #include "tracer_launch.h"
+#include "tracer_present.h"
+#include "bvh_wide.h"
 
 using namespace vkt;
 
@@ -42,14 +44,19 @@ template <class T> struct DevBuf {
 
 struct SceneBuffers {
     DevBuf<float4> tri, mats, sph_geo, sph_rec, planes, tri_nodes, sph_nodes;
+    DevBuf<float4> tri_wide, sph_wide;  // the BVHs as 4-wide nodes
     DevBuf<uint32_t> sph_id, emit;
     uint32_t nt = 0, nm = 0, ns = 0, np = 0, ne = 0;
     uint32_t n_tri_nodes = 0, n_sph_nodes = 0;
-    uint32_t depth = 0;  // deepest BVH
+    uint32_t depth = 0;       // deepest BVH
+    uint32_t wide_depth = 0;  // deepest 4-wide BVH
+    bool wide = false;        // 4-wide nodes present
     bool bvh = false;
     bool loaded = false;
     void release()
     {
+        tri_wide.release();
+        sph_wide.release();
         tri.release();
         mats.release();
         sph_geo.release();
@@ -67,8 +74,10 @@ struct AdjBuffers {
     DevBuf<float4> dldi, lin;
     DevBuf<double> grad;  // FP64 sums the kernel accumulates into
     DevBuf<float> gradf;  // the same, rounded to float for the outputs
+    DevBuf<float4> pix;   // wavefront form: per-pixel delta and sample-start RNG state
     void release()
     {
+        pix.release();
         dldi.release();
         lin.release();
         grad.release();
@@ -127,6 +136,17 @@ struct tracer_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<uint64_t> graph_key;
     AdjBuffers adj;  // adjoint: dL/dI, linear image and gradient buffers
+    // present pass and draw loop
+    uint64_t scene_version = 0;       // bumped by every scene or material upload
+    DevBuf<uchar4> slot[2];           // frame image slots (the reference's traced_images)
+    uint32_t slot_w = 0, slot_h = 0;
+    uint64_t draw_frame = 0;          // frames drawn since the last reset
+    DevBuf<float4> acc_sum, acc_disp[2];
+    uint32_t acc_n = 0;               // frames in acc_sum
+    tracer_frame acc_frame;           // what the accumulated frames share
+    tracer_trace_params acc_params;
+    uint64_t acc_version = 0;
+    DevBuf<unsigned char> pres_src[2], pres_out;  // staging for host images
 };
 
 namespace {
@@ -244,8 +264,10 @@ cudaEvent_t prof_event(tracer_ctx* c, size_t i)
 // Launches the wavefront: generate, then rounds of extend + shade until the
 // path queue is empty (read back a few rounds behind the launches) or
 // max_rounds is reached (no path needs more than spp * max_depth rounds).
+// With adj, the adjoint's generate and shade stages run instead of the
+// forward ones (the extend stage is shared).
 int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots, uint64_t max_rounds,
-                  uint32_t stack, uint32_t wavefront, cudaStream_t st)
+                  uint32_t stack, uint32_t wavefront, cudaStream_t st, const AdjWf* adj = nullptr)
 {
     WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
                c->wf_prim0.p, {c->wf_q0.p, c->wf_q1.p}, c->wf_count.p, c->wf_scene.p};
@@ -255,14 +277,20 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     wc.extend_grid = (uint32_t)(per * c->sm_count);
     const size_t sg = (nslots + 255) / 256;
     wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
-    cudaError_t e = wf_launch_generate(a, ws, wc, st);
+    cudaError_t e = cudaSuccess;
+    if (adj) {
+        e = cudaMemsetAsync(c->wf_count.p, 0, 3 * sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = wf_launch_adj_generate(a, ws, *adj, st);
+    } else {
+        e = wf_launch_generate(a, ws, wc, st);
+    }
     c->last_launches += 1;
     for (uint64_t r = 0; r < max_rounds && e == cudaSuccess; ++r) {
         const int qsel = (int)(r & 1);
         if (c->profiling) cudaEventRecord(prof_event(c, 3 * r), st);
         e = wf_launch_extend(a, ws, wc, qsel, st);
         if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 1), st);
-        if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, qsel, st);
+        if (e == cudaSuccess) e = adj ? wf_launch_adj_shade(a, ws, *adj, wc, qsel, st) : wf_launch_shade(a, ws, wc, qsel, st);
         if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 2), st);
         c->last_launches += 2;
         c->last_rounds = (uint32_t)(r + 1);
@@ -280,6 +308,33 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
         }
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
+    return TRACER_OK;
+}
+
+// Traversal width of the wavefront's extend kernel.  The 4-wide traversal
+// pushes up to three children per level, so it needs 3 x (its depth) stack
+// entries; with bvh_width = 0 it is used when the caller's stack (or, with
+// stack_depth = 0, that bound) allows, else the binary traversal runs.
+// stack: in, the binary traversal's stack; out, the stack of the chosen width.
+int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int& wide)
+{
+    wide = 0;
+    if (p->bvh_width != 0 && p->bvh_width != 2 && p->bvh_width != 4)
+        return fail(c, TRACER_ERR_INVALID_ARG, "bvh_width %u must be 0, 2 or 4", p->bvh_width);
+    const SceneBuffers& s = c->scene;
+    if (!s.bvh || !s.wide || p->bvh_width == 2) {
+        if (p->bvh_width == 4) return fail(c, TRACER_ERR_INVALID_ARG, "the scene has no 4-wide BVH");
+        return TRACER_OK;
+    }
+    const uint32_t need = 3 * s.wide_depth;
+    const uint32_t ws = p->stack_depth ? p->stack_depth : need;
+    if (ws < need || (size_t)ws * 256 * 8 > 200 * 1024) {
+        if (p->bvh_width == 4)
+            return fail(c, TRACER_ERR_STACK_OVERFLOW, "4-wide traversal needs a stack of %u entries", need);
+        return TRACER_OK;
+    }
+    stack = ws;
+    wide = 1;
     return TRACER_OK;
 }
 
@@ -372,6 +427,14 @@ void tracer_destroy(tracer_ctx* c)
     c->scene.release();
     c->batch.release();
     c->adj.release();
+    c->slot[0].release();
+    c->slot[1].release();
+    c->acc_sum.release();
+    c->acc_disp[0].release();
+    c->acc_disp[1].release();
+    c->pres_src[0].release();
+    c->pres_src[1].release();
+    c->pres_out.release();
     c->batch_slots.release();
     c->b_rgba8.release();
     c->b_rgba32f.release();
@@ -476,6 +539,12 @@ int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
     s.n_tri_nodes = (uint32_t)tnodes.size();
     s.n_sph_nodes = (uint32_t)snodes.size();
     s.depth = tdepth > sdepth ? tdepth : sdepth;
+    // the same BVHs as 4-wide nodes for the wavefront traversal
+    std::vector<WideNode> twide, swide;
+    uint32_t twd = 0, swd = 0;
+    const bool wide_ok = collapse_wide4(tnodes.data(), (uint32_t)tnodes.size(), twide, &twd) &&
+                         collapse_wide4(snodes.data(), (uint32_t)snodes.size(), swide, &swd);
+    s.wide_depth = twd > swd ? twd : swd;
 
     cudaError_t e = upload(s.tri, tri.data(), tri.size());
     if (e == cudaSuccess) e = upload(s.mats, reinterpret_cast<const float4*>(d->materials), 3 * (size_t)s.nm);
@@ -488,11 +557,17 @@ int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
         e = upload(s.tri_nodes, reinterpret_cast<const float4*>(tnodes.data()), 2 * tnodes.size());
     if (e == cudaSuccess)
         e = upload(s.sph_nodes, reinterpret_cast<const float4*>(snodes.data()), 2 * snodes.size());
+    if (e == cudaSuccess && wide_ok)
+        e = upload(s.tri_wide, reinterpret_cast<const float4*>(twide.data()), 8 * twide.size());
+    if (e == cudaSuccess && wide_ok)
+        e = upload(s.sph_wide, reinterpret_cast<const float4*>(swide.data()), 8 * swide.size());
     if (e != cudaSuccess) {
         s.release();
         return cuda_fail(c, e, "scene upload");
     }
+    s.wide = wide_ok;
     s.loaded = true;
+    ++c->scene_version;
     return TRACER_OK;
 }
 
@@ -505,6 +580,7 @@ int tracer_set_materials(tracer_ctx* c, const tracer_material* mats, uint32_t n)
     if (r != TRACER_OK) return r;
     cudaError_t e = cudaMemcpy(c->scene.mats.p, mats, sizeof(tracer_material) * n, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(c, e, "material update");
+    ++c->scene_version;
     return TRACER_OK;
 }
 
@@ -558,7 +634,8 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     std::memset(&a, 0, sizeof a);
     const SceneBuffers& s = c->scene;
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
-                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes};
+                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
+                    s.tri_wide.p, s.sph_wide.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     const tracer_camera& cam = f->camera;
@@ -610,7 +687,11 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         wc.stats = stats;
         wc.has_emitters = s.ne > 0;
         wc.block = p->block ? p->block : 128;
-        r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, stack, p->wavefront, st);
+        uint32_t wstack = stack;
+        r = pick_width(c, p, wstack, wc.wide);
+        if (r != TRACER_OK) return r;
+        a.stack_depth = wstack;
+        r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, st);
         if (r != TRACER_OK) return r;
     }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
@@ -782,7 +863,8 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     TraceArgs a;
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
-                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes};
+                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
+                    s.tri_wide.p, s.sph_wide.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
@@ -1289,6 +1371,23 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
     if ((size_t)stack * 128 * 8 > 100 * 1024)
         return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
+    // AUTO: below ~128k pixels the wavefront's per-round launches cost more
+    // than the per-pixel kernel's divergence (256^2 x 4 spp: 2.8 ms against
+    // 1.8 ms; 1024^2 x 64 spp: 5.8x faster as a wavefront)
+    const size_t npx_all = (size_t)p->width * p->height;
+    const int kernel = p->kernel == TRACER_KERNEL_AUTO
+                           ? (npx_all >= (1u << 17) ? TRACER_KERNEL_WAVEFRONT : TRACER_KERNEL_PLAIN)
+                           : p->kernel;
+    if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
+    const uint32_t wblock = p->block ? p->block : 128;
+    if (kernel == TRACER_KERNEL_WAVEFRONT && wblock != 64 && wblock != 128 && wblock != 256)
+        return fail(c, TRACER_ERR_INVALID_ARG, "wavefront block must be 64, 128 or 256");
+    // The wavefront form covers scenes without emissive spheres (no next-event
+    // estimation, zero camera gradient) given the forward linear image; the
+    // per-pixel kernel covers everything.
+    const bool use_wf = kernel == TRACER_KERNEL_WAVEFRONT && s.ne == 0 && linear_image != nullptr &&
+                        p->max_depth <= 1000 && p->spp < 32768u;
     int r = finish(c);
     if (r != TRACER_OK) return r;
     cudaSetDevice(c->device);
@@ -1318,7 +1417,8 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     TraceArgs a;
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
-                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes};
+                    s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
+                    s.tri_wide.p, s.sph_wide.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
@@ -1337,15 +1437,40 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     a.trav_limit = 2 * nn + 16;
     a.stats = c->stats.p;
     a.status = c->status.p;
-    c->last_kernel = 3;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
-    c->last_launches = 2;  // adjoint + FP64-to-float conversion
     c->last_mask = 1u << TRACER_AOV_STATS;
     c->width = p->width;
     c->height = p->height;
-    if (c->profiling) cudaEventRecord(c->prof_begin, st);
-    e = launch_adjoint(a, dldi, lin, ab.grad.p, s.nm, p->tie_mode, s.bvh ? 1 : 0, st);
+    if (use_wf) {
+        e = ensure_wavefront(c, npx);
+        if (e == cudaSuccess) e = dalloc(ab.pix, npx);
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront adjoint state allocation");
+        a.pixel_base = 0;
+        a.num_slots = (uint32_t)npx;
+        WfConfig wc;
+        std::memset(&wc, 0, sizeof wc);
+        wc.tie = p->tie_mode;
+        wc.bvh = s.bvh ? 1 : 0;
+        wc.stats = 1;
+        wc.block = wblock;
+        uint32_t wstack = stack;
+        r = pick_width(c, p, wstack, wc.wide);
+        if (r != TRACER_OK) return r;
+        a.stack_depth = wstack;
+        const AdjWf aw{dldi, lin, ab.grad.p, s.nm, ab.pix.p};
+        c->last_kernel = TRACER_KERNEL_WAVEFRONT;
+        c->last_launches = 1;  // + generate, rounds; the FP64-to-float conversion
+        if (c->profiling) cudaEventRecord(c->prof_begin, st);
+        // a sample takes at most max_depth rounds in each pass
+        r = run_wavefront(c, a, wc, npx, 2 * (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, st, &aw);
+        if (r != TRACER_OK) return r;
+    } else {
+        c->last_kernel = 3;
+        c->last_launches = 2;  // adjoint + FP64-to-float conversion
+        if (c->profiling) cudaEventRecord(c->prof_begin, st);
+        e = launch_adjoint(a, dldi, lin, ab.grad.p, s.nm, p->tie_mode, s.bvh ? 1 : 0, st);
+    }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
     if (e == cudaSuccess) e = launch_grad_to_float(ab.grad.p, ab.gradf.p, (uint32_t)ng, st);
     if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
@@ -1376,5 +1501,182 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
                 if (e != cudaSuccess) return cuda_fail(c, e, "gradient readback");
             }
     }
+    return TRACER_OK;
+}
+
+// ------------------------------------------------------------------ present
+namespace {
+
+int check_present(tracer_ctx* c, const tracer_present_params* pp, size_t out_bytes)
+{
+    if (!pp) return fail(c, TRACER_ERR_INVALID_ARG, "null present params");
+    if (pp->width == 0 || pp->height == 0 || pp->width > 32768 || pp->height > 32768)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "framebuffer %ux%u not supported", pp->width, pp->height);
+    if (pp->out_aov != TRACER_AOV_RGBA8 && pp->out_aov != TRACER_AOV_RGBA32F)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "present output must be RGBA8 or RGBA32F");
+    const size_t need = (size_t)pp->width * pp->height * (pp->out_aov == TRACER_AOV_RGBA8 ? 4 : 16);
+    if (out_bytes < need) return fail(c, TRACER_ERR_INVALID_ARG, "output holds %zu bytes, needs %zu", out_bytes, need);
+    return TRACER_OK;
+}
+
+// The present pass from device images into out (device: asynchronous; host:
+// through the staging buffer, waiting for the result).
+int present_into(tracer_ctx* c, const tracer_present_params* pp, const void* img0, const void* img1, uint32_t sw,
+                 uint32_t sh, int src_float, void* out, cudaStream_t st)
+{
+    const size_t bytes = (size_t)pp->width * pp->height * (pp->out_aov == TRACER_AOV_RGBA8 ? 4 : 16);
+    const bool dev_out = is_device_ptr(out);
+    void* dst = out;
+    cudaError_t e = cudaSuccess;
+    if (!dev_out) {
+        e = dalloc(c->pres_out, bytes);
+        dst = c->pres_out.p;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "present staging allocation");
+    PresentArgs pa{sw, sh, pp->width, pp->height,
+                   pp->out_aov == TRACER_AOV_RGBA8 ? static_cast<uchar4*>(dst) : nullptr,
+                   pp->out_aov == TRACER_AOV_RGBA32F ? static_cast<float4*>(dst) : nullptr};
+    e = launch_present(pa, img0, img1, src_float, st);
+    c->last_launches += 1;
+    if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "present launch");
+    c->pending = true;
+    if (!dev_out) {
+        int r = finish(c);
+        if (r != TRACER_OK) return r;
+        e = cudaMemcpy(out, dst, bytes, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(c, e, "present readback");
+    }
+    return TRACER_OK;
+}
+
+// Frame slots and accumulation buffers for w x h frames, cleared.
+cudaError_t reset_draw(tracer_ctx* c, uint32_t w, uint32_t h, cudaStream_t st)
+{
+    const size_t npx = (size_t)w * h;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+        e = dalloc(c->slot[k], npx);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->slot[k].p, 0, npx * sizeof(uchar4), st);
+    }
+    c->slot_w = w;
+    c->slot_h = h;
+    c->draw_frame = 0;
+    c->acc_n = 0;
+    return e;
+}
+
+}  // namespace
+
+extern "C" int tracer_present(tracer_ctx* c, const void* image0, const void* image1, uint32_t src_width,
+                              uint32_t src_height, int src_aov, const tracer_present_params* pp, void* out,
+                              size_t out_bytes, void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!image0 || !image1 || !out) return fail(c, TRACER_ERR_INVALID_ARG, "null image or output");
+    int r = check_present(c, pp, out_bytes);
+    if (r != TRACER_OK) return r;
+    if (src_aov != TRACER_AOV_RGBA8 && src_aov != TRACER_AOV_RGBA32F)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "source images must be RGBA8 or RGBA32F");
+    if (src_width == 0 || src_height == 0 || src_width > 32768 || src_height > 32768)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "source %ux%u not supported", src_width, src_height);
+    r = finish(c);  // the staging buffers may still be read by the last call
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    const size_t sbytes = (size_t)src_width * src_height * (src_aov == TRACER_AOV_RGBA8 ? 4 : 16);
+    const void* src[2] = {image0, image1};
+    for (int k = 0; k < 2; ++k) {
+        if (is_device_ptr(src[k])) continue;
+        cudaError_t e = dalloc(c->pres_src[k], sbytes);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->pres_src[k].p, src[k], sbytes, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "present source upload");
+        src[k] = c->pres_src[k].p;
+    }
+    c->last_launches = 0;
+    return present_into(c, pp, src[0], src[1], src_width, src_height, src_aov == TRACER_AOV_RGBA32F, out, st);
+}
+
+extern "C" int tracer_draw(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params* p,
+                           const tracer_present_params* pp, void* out, size_t out_bytes, void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!f || !p || !out) return fail(c, TRACER_ERR_INVALID_ARG, "null frame, params or output");
+    int r = check_present(c, pp, out_bytes);
+    if (r != TRACER_OK) return r;
+    if (pp->mode != TRACER_PRESENT_PINGPONG && pp->mode != TRACER_PRESENT_ACCUMULATE)
+        return fail(c, TRACER_ERR_INVALID_ARG, "unknown present mode %u", pp->mode);
+    const bool accumulate = pp->mode == TRACER_PRESENT_ACCUMULATE;
+    tracer_trace_params q = *p;
+    q.aov_mask = (q.aov_mask ? q.aov_mask : (1u << TRACER_AOV_RGBA8)) | (1u << TRACER_AOV_RGBA8) |
+                 (accumulate ? 1u << TRACER_AOV_LINEAR : 0u);
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    const size_t npx = (size_t)q.width * q.height;
+    if (q.width != c->slot_w || q.height != c->slot_h || !c->slot[0].p) {
+        r = finish(c);
+        if (r != TRACER_OK) return r;
+        cudaSetDevice(c->device);
+        cudaError_t e = reset_draw(c, q.width, q.height, st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "frame slot allocation");
+    }
+    r = tracer_trace(c, f, &q, cuda_stream);
+    if (r != TRACER_OK) return r;
+    cudaError_t e = cudaSuccess;
+    if (!accumulate) {
+        // frame k's image goes to slot k % 2; the pass reads the slots as bound
+        const int s = (int)(c->draw_frame & 1);
+        e = cudaMemcpyAsync(c->slot[s].p, c->rgba8.p, npx * sizeof(uchar4), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "frame slot copy");
+        r = present_into(c, pp, c->slot[0].p, c->slot[1].p, q.width, q.height, 0, out, st);
+    } else {
+        // the camera's four vectors, bit for bit (not its padding lanes)
+        const tracer_camera &ca = c->acc_frame.camera, &cb = f->camera;
+        const bool same_cam = std::memcmp(ca.pos, cb.pos, sizeof ca.pos) == 0 &&
+                              std::memcmp(ca.dir, cb.dir, sizeof ca.dir) == 0 &&
+                              std::memcmp(ca.right, cb.right, sizeof ca.right) == 0 &&
+                              std::memcmp(ca.up, cb.up, sizeof ca.up) == 0;
+        const bool same = c->acc_n > 0 && c->acc_version == c->scene_version &&
+                          c->acc_frame.aspect_ratio == f->aspect_ratio && same_cam &&
+                          c->acc_params.spp == q.spp && c->acc_params.max_depth == q.max_depth &&
+                          c->acc_params.rr_start == q.rr_start && c->acc_params.tie_mode == q.tie_mode &&
+                          std::memcmp(c->acc_params.sky, q.sky, sizeof q.sky) == 0;
+        if (!same) {
+            e = dalloc(c->acc_sum, npx);
+            if (e == cudaSuccess) e = dalloc(c->acc_disp[0], npx);
+            if (e == cudaSuccess) e = dalloc(c->acc_disp[1], npx);
+            if (e == cudaSuccess) e = cudaMemsetAsync(c->acc_sum.p, 0, npx * sizeof(float4), st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(c->acc_disp[0].p, 0, npx * sizeof(float4), st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(c->acc_disp[1].p, 0, npx * sizeof(float4), st);
+            if (e != cudaSuccess) return cuda_fail(c, e, "accumulation buffers");
+            c->acc_n = 0;
+            c->acc_frame = *f;
+            c->acc_params = q;
+            c->acc_version = c->scene_version;
+        }
+        ++c->acc_n;
+        const int cur = (int)(c->acc_n & 1);
+        e = launch_accumulate(c->linear.p, c->acc_sum.p, c->acc_disp[cur].p, (uint32_t)npx, c->acc_n, c->sm_count,
+                              st);
+        c->last_launches += 1;
+        if (e != cudaSuccess) return cuda_fail(c, e, "accumulate launch");
+        r = present_into(c, pp, c->acc_disp[cur].p, c->acc_disp[cur ^ 1].p, q.width, q.height, 1, out, st);
+    }
+    if (r == TRACER_OK) ++c->draw_frame;
+    return r;
+}
+
+extern "C" int tracer_draw_reset(tracer_ctx* c)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    if (c->slot_w && c->slot_h) {
+        cudaError_t e = reset_draw(c, c->slot_w, c->slot_h, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "draw reset");
+    }
+    c->draw_frame = 0;
+    c->acc_n = 0;
     return TRACER_OK;
 }

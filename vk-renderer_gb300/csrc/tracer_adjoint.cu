@@ -37,6 +37,7 @@
 
 #include "tracer_core.cuh"
 #include "tracer_launch.h"
+#include "tracer_wavefront.h"
 
 namespace vkt {
 
@@ -194,6 +195,23 @@ __device__ __forceinline__ V3 nee_one_grad(TR& tr, const TraceArgs& a, uint32_t 
     return base * att * NdotL;
 }
 
+// tonemap(x) = (x / (x + 1))^(1/2.2) has slope g (x/(x+1))^(g-1) / (x+1)^2,
+// infinite at 0: the slope is taken at x >= 1e-6.
+__device__ __forceinline__ float tm_slope(float x)
+{
+    const float gam = 1.0f / 2.2f;
+    x = gmax(x, 1e-6f);
+    const float r = x / (x + 1.0f);
+    return gam * powf(r, gam - 1.0f) / ((x + 1.0f) * (x + 1.0f));
+}
+
+// delta = dL/dI * tonemap'(accum / spp) / spp per channel: the weight of one
+// sample's radiance in the loss.
+__device__ __forceinline__ V3 pixel_delta(float4 dl, V3 lin, uint32_t spp)
+{
+    return v3(dl.x * tm_slope(lin.x), dl.y * tm_slope(lin.y), dl.z * tm_slope(lin.z)) / (float)spp;
+}
+
 // Pass 1: the radiance loop with clamp bookkeeping.  lc[c] = last depth whose
 // clamp of acc[c] was active (-1: none); T = contributions that survive.
 template <class TR>
@@ -254,16 +272,7 @@ __global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
             for (uint32_t s = 0; s < a.spp; ++s) acc = acc + radiance(tr, a, pr, g0, nullptr, nullptr);
             lin = acc / (float)a.spp;
         }
-        const float4 dl = ga.dldi[i];
-        // tonemap(x) = (x / (x + 1))^(1/2.2): slope g (x/(x+1))^(g-1) / (x+1)^2
-        // (infinite at 0: the slope is taken at x >= 1e-6)
-        const float gam = 1.0f / 2.2f;
-        auto tm_slope = [&](float xx) {
-            xx = gmax(xx, 1e-6f);
-            const float r = xx / (xx + 1.0f);
-            return gam * powf(r, gam - 1.0f) / ((xx + 1.0f) * (xx + 1.0f));
-        };
-        const V3 delta = v3(dl.x * tm_slope(lin.x), dl.y * tm_slope(lin.y), dl.z * tm_slope(lin.z)) / (float)a.spp;
+        const V3 delta = pixel_delta(ga.dldi[i], lin, a.spp);
         if (finite3(delta) && finite3(lin)) {
             for (uint32_t s = 0; s < a.spp; ++s) {
                 const Rng gs = g;  // this sample's RNG state
@@ -410,6 +419,239 @@ __global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
         for (uint32_t k = tid; k < ngrad; k += nthreads)
             if (sgrad[k] != 0.0) atomicAdd(ga.grad + k, sgrad[k]);
     }
+}
+
+// ------------------------------------------------------ wavefront adjoint --
+// The same two passes per sample for scenes without emissive spheres, as
+// stages over the wavefront's path queue: the closest-hit rays of both passes
+// go through the forward renderer's extend kernel, and wf_adj_shade runs one
+// bounce of whichever pass a path is in.  A path's state between rounds:
+//   ray_o/ray_d  the ray to trace next (tmax in ray_o.w)
+//   acc          pass 1: acc; pass 2: the surviving prefix; .w the RNG salt
+//   mask         mask; .w the three last-clamp depths (10 bits each, +1)
+//   accum        T (pass 2 reads it); .w phase << 31 | sample << 16 | depth
+//   pix          delta of the pixel; .w the RNG salt at the sample's start
+//   prim0        the RNG salt at the sample's end (pass 2 restores it)
+// Without emitters the camera position enters radiance only through which
+// primitives are hit, so its gradient is zero.
+
+__device__ __forceinline__ uint32_t lc_pack(const int lc[3])
+{
+    return (uint32_t)(lc[0] + 1) | ((uint32_t)(lc[1] + 1) << 10) | ((uint32_t)(lc[2] + 1) << 20);
+}
+__device__ __forceinline__ void lc_unpack(uint32_t v, int lc[3])
+{
+    lc[0] = (int)(v & 0x3FFu) - 1;
+    lc[1] = (int)((v >> 10) & 0x3FFu) - 1;
+    lc[2] = (int)((v >> 20) & 0x3FFu) - 1;
+}
+constexpr uint32_t kPhaseReplay = 1u << 31;
+
+__global__ void __launch_bounds__(256) wf_adj_generate(TraceArgs a, WfState s, AdjWf w)
+{
+    const uint32_t n = a.width * a.height;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool queued = false;
+    if (i < n) {
+        const uint32_t x = i % a.width, y = i / a.width;
+        const V3 lin = v3(w.linear[i]);
+        const V3 delta = pixel_delta(w.dldi[i], lin, a.spp);
+        if (finite3(delta) && finite3(lin)) {  // as the per-pixel kernel: other pixels trace nothing
+            Rng g;
+            seed_rng(a, x, y, g);
+            const Ray r = primary_ray(a, x, y);
+            const int none[3] = {-1, -1, -1};
+            s.ray_o[i] = make_float4(r.o.x, r.o.y, r.o.z, depth_tmax(0));
+            s.ray_d[i] = make_float4(r.d.x, r.d.y, r.d.z, 0.0f);
+            s.acc[i] = make_float4(0.0f, 0.0f, 0.0f, g.salt);
+            s.mask[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(lc_pack(none)));
+            s.accum[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0u));
+            w.pix[i] = make_float4(delta.x, delta.y, delta.z, g.salt);
+            queued = true;
+        }
+    }
+    warp_append(queued, i, s.queue[0], &s.count[0]);
+}
+
+// d/da_m[c] += delta[c] R[c] / a_m[c] for the material a path just scattered on.
+__device__ __forceinline__ void albedo_grad(double* gal, int m, V3 delta, V3 R, V3 albedo)
+{
+    if (albedo.x != 0.0f) gadd(gal, 3 * m + 0, delta.x * R.x / albedo.x);
+    if (albedo.y != 0.0f) gadd(gal, 3 * m + 1, delta.y * R.y / albedo.y);
+    if (albedo.z != 0.0f) gadd(gal, 3 * m + 2, delta.z * R.z / albedo.z);
+}
+
+template <int TIE, bool BVH>
+__global__ void __launch_bounds__(256) wf_adj_shade(TraceArgs a, WfState s, AdjWf w, int qsel)
+{
+    const uint32_t n = s.count[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
+    uint32_t* next = qsel ? s.queue[0] : s.queue[1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // extend's fetch cursor for the next round
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    // no emitters: shading traces no shadow rays and needs no stack
+    Tracer<TIE, BVH, false> tr{a.sc, Stack{nullptr, nullptr, 0, 0}, cnt, a.status, a.trav_limit};
+    double* gal = w.grad;
+    double* gem = w.grad + 3 * (size_t)w.nm;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t qi = base + threadIdx.x;
+        bool again = false;
+        uint32_t pid = 0;
+        if (qi < n) {
+            pid = queue[qi];
+            const uint32_t x = pid % a.width, y = pid / a.width;
+            const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
+            const uint4 hr = s.hit[pid];
+            const float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
+            const uint32_t bits = __float_as_uint(accum4.w);
+            bool replay = (bits & kPhaseReplay) != 0;
+            uint32_t sample = (bits >> 16) & 0x7FFFu, depth = bits & 0xFFFFu;
+            int lc[3];
+            lc_unpack(__float_as_uint(mask4.w), lc);
+            Rng g;
+            g.salt = acc4.w;
+            g.cx = (float)x / (float)a.width;
+            g.cy = (float)y / (float)a.height;
+            Hit h;
+            h.t = __uint_as_float(hr.x);
+            h.prim = hr.y;
+            h.slot = hr.z;
+            h.kind = (int)hr.w;
+            const bool found = h.kind != 0;
+            Ray ray{v3(ro), v3(rd)};
+            V3 acc = v3(acc4), mask = v3(mask4), T = v3(accum4);
+            float start_salt = 0.0f;
+            bool pix_dirty = false;
+            if (!replay) {
+                // pass 1: clamp bookkeeping, then the forward bounce
+                if (acc.x < 0.0f || acc.x > 1.0f) { lc[0] = (int)depth; T.x = 0.0f; }
+                if (acc.y < 0.0f || acc.y > 1.0f) { lc[1] = (int)depth; T.y = 0.0f; }
+                if (acc.z < 0.0f || acc.z > 1.0f) { lc[2] = (int)depth; T.z = 0.0f; }
+                acc = vclamp01(acc);
+                const V3 before = acc;
+                const bool cont = shade_bounce(tr, a, depth, found, h, ray, acc, mask, g);
+                T = T + (acc - before);
+                depth++;
+                if (cont && depth < a.max_depth) {
+                    again = true;
+                } else {  // pass 2 of the same sample: its first ray and RNG state again
+                    s.prim0[pid] = __float_as_uint(g.salt);
+                    g.salt = w.pix[pid].w;
+                    ray = primary_ray(a, x, y);
+                    acc = splat(0.0f);
+                    mask = splat(1.0f);
+                    depth = 0;
+                    replay = true;
+                    again = true;
+                }
+            } else {
+                // pass 2: the same bounce, with its gradient terms
+                const V3 delta = v3(w.pix[pid]);
+                const V3 surv = v3((int)depth >= lc[0] ? 1.0f : 0.0f, (int)depth >= lc[1] ? 1.0f : 0.0f,
+                                   (int)depth >= lc[2] ? 1.0f : 0.0f);
+                const V3 wgt = delta * surv;
+                bool cont = false;
+                if (found) {
+                    V3 P, N;
+                    Material mat;
+                    tr.surface(ray, h, P, N, mat);
+                    const int m = h.kind == 1 ? (int)__float_as_uint(__ldg(a.sc.tri + 3 * (size_t)h.slot).w) : -1;
+                    if (mat.type == MAT_DIFFUSE) {
+                        const float r2 = rand01(g);
+                        const V3 d = jitter(N, (2.0f * PI) * rand01(g), sqrtf(r2), sqrtf(1.0f - r2)) *
+                                     (1.0f - mat.metalness);
+                        const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
+                        const V3 en = emits ? normalize(mat.emissive) : splat(0.0f);
+                        if (m >= 0 && emits) {  // d normalize(e) = (I - n n^T) / |e|
+                            const V3 wm = wgt * mask;
+                            const V3 ge = (wm - en * dot(en, wm)) * (1.0f / length(mat.emissive));
+                            gadd(gem, 3 * m + 0, ge.x);
+                            gadd(gem, 3 * m + 1, ge.y);
+                            gadd(gem, 3 * m + 2, ge.z);
+                        }
+                        acc = acc + mask * en * surv;
+                        if (m >= 0) albedo_grad(gal, m, delta, T - acc, mat.albedo);
+                        mask = mask * mat.albedo;
+                        ray = Ray{P, normalize(reflect(ray.d, N) + d)};
+                    } else if (mat.type == MAT_DIELECTRIC) {
+                        if (m >= 0) {
+                            const V3 ge = wgt * mask;
+                            gadd(gem, 3 * m + 0, ge.x);
+                            gadd(gem, 3 * m + 1, ge.y);
+                            gadd(gem, 3 * m + 2, ge.z);
+                        }
+                        acc = acc + mat.emissive * mask * surv;
+                        if (m >= 0) albedo_grad(gal, m, delta, T - acc, mat.albedo);
+                        mask = mask * mat.albedo;
+                        const float cosine = -dot(ray.d, N) / length(ray.d);
+                        const V3 reflected = reflect(ray.d, N);
+                        const V3 refracted = refract(ray.d, N, mat.roughness);
+                        const float prob = (refracted == splat(0.0f)) ? 1.0f : schlick(cosine, mat.roughness);
+                        ray = Ray{P, normalize(rand01(g) < prob ? reflected : refracted)};
+                    }
+                    cont = true;
+                    if (depth >= a.rr_start) {
+                        const float p = max3(mask);
+                        if (rand01(g) > p)
+                            cont = false;
+                        else
+                            mask = mask * (1.0f / p);
+                    }
+                }
+                depth++;
+                if (cont && depth < a.max_depth) {
+                    again = true;
+                } else {  // sample finished: the RNG continues where pass 1 left it
+                    g.salt = __uint_as_float(s.prim0[pid]);
+                    sample++;
+                    if (sample < a.spp) {
+                        ray = primary_ray(a, x, y);
+                        acc = splat(0.0f);
+                        mask = splat(1.0f);
+                        T = splat(0.0f);
+                        lc[0] = lc[1] = lc[2] = -1;
+                        depth = 0;
+                        replay = false;
+                        start_salt = g.salt;
+                        pix_dirty = true;
+                        again = true;
+                    }
+                }
+            }
+            if (again) {
+                s.ray_o[pid] = make_float4(ray.o.x, ray.o.y, ray.o.z, depth_tmax(depth));
+                s.ray_d[pid] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
+                s.acc[pid] = make_float4(acc.x, acc.y, acc.z, g.salt);
+                s.mask[pid] = make_float4(mask.x, mask.y, mask.z, __uint_as_float(lc_pack(lc)));
+                s.accum[pid] = make_float4(T.x, T.y, T.z,
+                                           __uint_as_float((replay ? kPhaseReplay : 0u) | (sample << 16) | depth));
+                if (pix_dirty) w.pix[pid].w = start_salt;
+            }
+        }
+        warp_append(again, pid, next, &s.count[qsel ^ 1]);
+    }
+}
+
+cudaError_t wf_launch_adj_generate(const TraceArgs& a, const WfState& s, const AdjWf& w, cudaStream_t st)
+{
+    const uint32_t n = a.width * a.height;
+    wf_adj_generate<<<(n + 255) / 256, 256, 0, st>>>(a, s, w);
+    return cudaGetLastError();
+}
+
+cudaError_t wf_launch_adj_shade(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
+                                cudaStream_t st)
+{
+    if (c.tie == TIE_REFERENCE)
+        wf_adj_shade<TIE_REFERENCE, false><<<c.shade_grid, 256, 0, st>>>(a, s, w, qsel);
+    else if (c.bvh)
+        wf_adj_shade<TIE_STRICT, true><<<c.shade_grid, 256, 0, st>>>(a, s, w, qsel);
+    else
+        wf_adj_shade<TIE_STRICT, false><<<c.shade_grid, 256, 0, st>>>(a, s, w, qsel);
+    return cudaGetLastError();
 }
 
 template <int TIE, bool BVH, bool CAM>

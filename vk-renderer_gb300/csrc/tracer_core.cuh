@@ -446,4 +446,20 @@ __device__ __forceinline__ void flush_counters(const TraceArgs& a, Counters& cnt
     }
 }
 
+// Warp-level compaction: the lanes with want = true write value to
+// consecutive entries of queue, reserved with one atomicAdd on count per warp.
+// Every lane of the warp must call it.
+__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* queue, uint32_t* count)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const unsigned m = __ballot_sync(full, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(full, base, leader);
+    if (want) queue[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
 }  // namespace vkt

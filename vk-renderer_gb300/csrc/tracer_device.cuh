@@ -196,6 +196,8 @@ struct DevScene {
     const float4* sph_nodes;
     uint32_t nt, nm, ns, np, ne;
     uint32_t n_tri_nodes, n_sph_nodes;
+    const float4* tri_wide;  // 4-wide nodes (8 float4 each) of the same BVHs, or NULL
+    const float4* sph_wide;
 };
 
 struct Counters {
@@ -296,15 +298,20 @@ __device__ __forceinline__ float fmax3(float a, float b, float c)
 // max(min(z0,z1), 0)), tmax = min(min(max(x0,x1), max(y0,y1)),
 // min(max(z0,z1), tbest)); hit iff tmin <= tmax * (1 + 2^-20).  Rays with a
 // NaN direction never reach this test.
-__device__ __forceinline__ bool box_hit(const BoxRay& r, float4 lo, float4 hi, float tbest, float& tnear)
+__device__ __forceinline__ bool box_hit_s(const BoxRay& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                          float tbest, float& tnear)
 {
-    float x0 = __fmaf_rn(lo.x, r.ix, r.nx), x1 = __fmaf_rn(hi.x, r.ix, r.nx);
-    float y0 = __fmaf_rn(lo.y, r.iy, r.ny), y1 = __fmaf_rn(hi.y, r.iy, r.ny);
-    float z0 = __fmaf_rn(lo.z, r.iz, r.nz), z1 = __fmaf_rn(hi.z, r.iz, r.nz);
+    float x0 = __fmaf_rn(lx, r.ix, r.nx), x1 = __fmaf_rn(hx, r.ix, r.nx);
+    float y0 = __fmaf_rn(ly, r.iy, r.ny), y1 = __fmaf_rn(hy, r.iy, r.ny);
+    float z0 = __fmaf_rn(lz, r.iz, r.nz), z1 = __fmaf_rn(hz, r.iz, r.nz);
     float tmin = fmaxf(fmax3(fminf(x0, x1), fminf(y0, y1), fminf(z0, z1)), 0.0f);
     float tmax = fminf(fmin3(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1)), tbest);
     tnear = tmin;
     return tmin <= tmax * BOX_SLACK;
+}
+__device__ __forceinline__ bool box_hit(const BoxRay& r, float4 lo, float4 hi, float tbest, float& tnear)
+{
+    return box_hit_s(r, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tbest, tnear);
 }
 
 }  // namespace vkt

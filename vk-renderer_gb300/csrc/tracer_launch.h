@@ -24,4 +24,18 @@ cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4*
 // out[i] = (float)g[i], i < n
 cudaError_t launch_grad_to_float(const double* g, float* out, uint32_t n, cudaStream_t s);
 
+// Wavefront adjoint (scenes without emissive spheres): per-pixel inputs and
+// outputs beside the wavefront state.
+struct AdjWf {
+    const float4* dldi;    // dL/dI per pixel
+    const float4* linear;  // accum / spp per pixel from the forward trace
+    double* grad;          // [nm x 3 albedo][nm x 3 emission][3 camera position]
+    uint32_t nm;
+    float4* pix;           // per pixel: delta, RNG salt at the current sample's start
+};
+// Seeds every pixel with a finite delta and queues it in queue 0 (counts must be zero).
+cudaError_t wf_launch_adj_generate(const TraceArgs& a, const WfState& s, const AdjWf& w, cudaStream_t st);
+cudaError_t wf_launch_adj_shade(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
+                                cudaStream_t st);
+
 }  // namespace vkt

@@ -56,19 +56,6 @@ __device__ __forceinline__ int child_enc(float4 lo, float4 hi)
     return cnt > 0 ? leaf_enc(left, cnt) : left;
 }
 
-__device__ __forceinline__ void warp_append(bool want, uint32_t value, uint32_t* queue, uint32_t* count)
-{
-    const unsigned full = 0xFFFFFFFFu;
-    const unsigned m = __ballot_sync(full, want);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(full, base, leader);
-    if (want) queue[base + __popc(m & ((1u << lane) - 1u))] = value;
-}
-
 // The TraceArgs a path belongs to: the launch's own (single scene) or its
 // scene's entry in the table (batched).
 #define SCENE_ARGS(MULTI, a, slots, sid) ((MULTI) ? (slots)[(sid)] : (a))
@@ -151,23 +138,6 @@ __device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, 
     }
 }
 
-template <bool STATS>
-__device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters& cnt)
-{
-    L.nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
-    L.prims = L.pass == 0 ? sc.tri : sc.sph_geo;
-    const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
-    if (STATS) cnt.c[C_NODES]++;
-    float tn;
-    L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? child_enc(lo, hi) : 0;
-    L.leaf = 0;
-    L.sp = 0;
-    if (L.cur < 0) {  // the root is a leaf
-        L.leaf = L.cur;
-        L.cur = 0;
-    }
-}
-
 __device__ __forceinline__ int pop(Lane& L, const Stack& stk)
 {
     while (L.sp > 0) {
@@ -179,8 +149,91 @@ __device__ __forceinline__ int pop(Lane& L, const Stack& stk)
     return 0;
 }
 
-template <int TIE, bool STATS, bool MULTI, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
+__device__ __forceinline__ void push(Lane& L, const Stack& stk, int e, float tn, int* status)
+{
+    if (L.sp >= stk.cap) {
+        atomicCAS(status, ST_OK, ST_STACK_OVERFLOW);
+        return;
+    }
+    stk.ci[L.sp * stk.stride] = e;
+    stk.tn[L.sp * stk.stride] = tn;
+    ++L.sp;
+}
+
+__device__ __forceinline__ void order2(float& ta, int& ra, float& tb, int& rb)
+{
+    if (tb < ta) {
+        const float t = ta;
+        ta = tb;
+        tb = t;
+        const int r = ra;
+        ra = rb;
+        rb = r;
+    }
+}
+
+// One 4-wide node: the slab test of each child's box (the binary node's box,
+// the same test as box_hit), the nearest child hit becomes the next
+// reference, the others are pushed farthest first.  Which boxes are tested
+// differs from the binary traversal only in order and in skipping interior
+// boxes, so the closest hit under strict ties is the same.
+template <bool STATS>
+__device__ __forceinline__ void visit_wide(Lane& L, int w, const Stack& stk, int* status, Counters& cnt)
+{
+    const float4* n = L.nodes + 8 * (size_t)w;
+    const float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
+    const float4 lz = __ldg(n + 4), hz = __ldg(n + 5);
+    const int4 ch = __ldg(reinterpret_cast<const int4*>(n + 6));
+    const float INF = __int_as_float(0x7f800000);
+    float t0, t1, t2, t3;
+    int r0 = ch.x, r1 = ch.y, r2 = ch.z, r3 = ch.w;
+    if (STATS) cnt.c[C_NODES] += (r0 != 0) + (r1 != 0) + (r2 != 0) + (r3 != 0);
+    if (!(r0 != 0 && box_hit_s(L.br, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, L.h.t, t0))) { t0 = INF; r0 = 0; }
+    if (!(r1 != 0 && box_hit_s(L.br, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, L.h.t, t1))) { t1 = INF; r1 = 0; }
+    if (!(r2 != 0 && box_hit_s(L.br, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, L.h.t, t2))) { t2 = INF; r2 = 0; }
+    if (!(r3 != 0 && box_hit_s(L.br, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, L.h.t, t3))) { t3 = INF; r3 = 0; }
+    // sorting network: ascending distance (misses last)
+    order2(t0, r0, t1, r1);
+    order2(t2, r2, t3, r3);
+    order2(t0, r0, t2, r2);
+    order2(t1, r1, t3, r3);
+    order2(t1, r1, t2, r2);
+    if (r3) push(L, stk, r3, t3, status);
+    if (r2) push(L, stk, r2, t2, status);
+    if (r1) push(L, stk, r1, t1, status);
+    L.cur = r0 ? r0 : pop(L, stk);
+}
+
+template <bool STATS, bool WIDE>
+__device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters& cnt, const Stack& stk, int* status)
+{
+    L.prims = L.pass == 0 ? sc.tri : sc.sph_geo;
+    L.leaf = 0;
+    L.sp = 0;
+    if (WIDE) {
+        L.nodes = L.pass == 0 ? sc.tri_wide : sc.sph_wide;
+        visit_wide<STATS>(L, 0, stk, status, cnt);
+        if (L.cur < 0) {
+            L.leaf = L.cur;
+            L.cur = pop(L, stk);
+        }
+        return;
+    }
+    L.nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
+    const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
+    if (STATS) cnt.c[C_NODES]++;
+    float tn;
+    L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? child_enc(lo, hi) : 0;
+    if (L.cur < 0) {  // the root is a leaf
+        L.leaf = L.cur;
+        L.cur = 0;
+    }
+}
+
+// 1024 resident threads per SM for the binary traversal (64 registers); the
+// 4-wide node visit holds four boxes at once and gets 80 (768 threads).
+template <int TIE, bool STATS, bool MULTI, int BLOCK, bool WIDE>
+__global__ void __launch_bounds__(BLOCK, (WIDE ? 768 : 1024) / BLOCK)
     wf_extend_bvh(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
     extern __shared__ int smem[];
@@ -235,7 +288,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     } else {
                         L.br = make_boxray(Ray{L.o, L.d});
                         L.pass = has_tri ? 0 : 1;
-                        start_pass<STATS>(sc, L, cnt);
+                        start_pass<STATS, WIDE>(sc, L, cnt, stk, a.status);
                     }
                 }
             }
@@ -255,6 +308,12 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     L.cur = 0;
                     L.leaf = 0;
                     L.sp = 0;
+                } else if (WIDE) {
+                    visit_wide<STATS>(L, L.cur, stk, a.status, cnt);
+                    if (L.cur < 0 && L.leaf == 0) {
+                        L.leaf = L.cur;
+                        L.cur = pop(L, stk);
+                    }
                 } else {
                     const float4* c = L.nodes + 2 * (size_t)L.cur;
                     const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
@@ -335,7 +394,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
             const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
             if (L.pass == 0 && sc.n_sph_nodes > 0 && sc.ns > 0) {
                 L.pass = 1;
-                start_pass<STATS>(sc, L, cnt);
+                start_pass<STATS, WIDE>(sc, L, cnt, stk, a.status);
             } else {
                 planes_pass<STATS>(sc, Ray{L.o, L.d}, L.h, cnt);
                 if (STATS && L.h.kind) cnt.c[C_HITS]++;
@@ -472,7 +531,7 @@ static void smem_attr(K k, size_t smem)
 template <int TIE, bool STATS, bool MULTI, int BLOCK>
 static cudaError_t extend_bvh_b(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
-    auto k = wf_extend_bvh<TIE, STATS, MULTI, BLOCK>;
+    auto k = c.wide ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true> : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
     const size_t smem = (size_t)a.stack_depth * BLOCK * 8;
     smem_attr(k, smem);
     k<<<c.extend_grid, BLOCK, smem, st>>>(a, s, qsel, c.slots);
@@ -536,34 +595,36 @@ cudaError_t wf_launch_shade(const TraceArgs& a, const WfState& s, const WfConfig
     WF_DISPATCH(shade_t)
 }
 
+template <int TIE, bool STATS, bool MULTI, int BLOCK>
+static cudaError_t occ_bvh_b(int& n, bool wide, size_t smem)
+{
+    auto k = wide ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true> : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
+    smem_attr(k, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, BLOCK, smem);
+}
+
 template <int TIE, bool STATS, bool MULTI>
-static int occ_bvh(uint32_t block, size_t stack_depth)
+static int occ_bvh(uint32_t block, size_t stack_depth, bool wide)
 {
     int n = 0;
-    cudaError_t e;
     const size_t smem = stack_depth * block * 8;
-    if (block == 64) {
-        auto k = wf_extend_bvh<TIE, STATS, MULTI, 64>;
-        smem_attr(k, smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 64, smem);
-    } else if (block == 256) {
-        auto k = wf_extend_bvh<TIE, STATS, MULTI, 256>;
-        smem_attr(k, smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, smem);
-    } else {
-        auto k = wf_extend_bvh<TIE, STATS, MULTI, 128>;
-        smem_attr(k, smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, smem);
-    }
+    cudaError_t e;
+    if (block == 64)
+        e = occ_bvh_b<TIE, STATS, MULTI, 64>(n, wide, smem);
+    else if (block == 256)
+        e = occ_bvh_b<TIE, STATS, MULTI, 256>(n, wide, smem);
+    else
+        e = occ_bvh_b<TIE, STATS, MULTI, 128>(n, wide, smem);
     return e == cudaSuccess ? n : 0;
 }
 
 int wf_extend_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
 {
-    if (c.multi) return c.stats ? occ_bvh<TIE_STRICT, true, true>(c.block, stack_depth)
-                                : occ_bvh<TIE_STRICT, false, true>(c.block, stack_depth);
-    if (c.bvh) return c.stats ? occ_bvh<TIE_STRICT, true, false>(c.block, stack_depth)
-                              : occ_bvh<TIE_STRICT, false, false>(c.block, stack_depth);
+    const bool w = c.wide != 0;
+    if (c.multi) return c.stats ? occ_bvh<TIE_STRICT, true, true>(c.block, stack_depth, w)
+                                : occ_bvh<TIE_STRICT, false, true>(c.block, stack_depth, w);
+    if (c.bvh) return c.stats ? occ_bvh<TIE_STRICT, true, false>(c.block, stack_depth, w)
+                              : occ_bvh<TIE_STRICT, false, false>(c.block, stack_depth, w);
     int n = 0;
     cudaError_t e;
     if (c.tie == TIE_REFERENCE)

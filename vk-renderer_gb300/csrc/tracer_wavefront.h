@@ -27,6 +27,7 @@ struct WfConfig {
     int tie, bvh, stats;
     int multi;                // batched: per-slot scene table
     int has_emitters;         // some scene has emissive spheres (shade needs a traversal stack)
+    int wide;                 // extend traverses the 4-wide nodes (every scene has them)
     uint32_t block;           // extend kernel threads per block: 64, 128 or 256
     uint32_t extend_grid, shade_grid;
     const TraceArgs* slots;   // batched: device table of per-scene arguments

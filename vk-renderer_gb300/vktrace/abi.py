@@ -39,8 +39,12 @@ EXPORTED_SYMBOLS = [
     "tracer_upload_scene", "tracer_set_materials", "tracer_trace", "tracer_readback", "tracer_synchronize",
     "tracer_device_image", "tracer_build_bvh", "tracer_validate_bvh", "tracer_set_profiling",
     "tracer_last_timings", "tracer_trace_noalloc", "tracer_upload_scenes", "tracer_trace_batched",
-    "tracer_readback_scene", "tracer_trace_adjoint",
+    "tracer_readback_scene", "tracer_trace_adjoint", "tracer_present", "tracer_draw", "tracer_draw_reset",
+    "tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update", "tracer_camera_move",
+    "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script",
 ]
+PRESENT_PINGPONG, PRESENT_ACCUMULATE = 0, 1
+KEY_W, KEY_S, KEY_A, KEY_D, KEY_R, KEY_F = 1, 2, 4, 8, 16, 32
 NOALLOC_MAX_PIXELS = 16384
 NOALLOC_MAX_ROUNDS = 8192
 
@@ -70,8 +74,24 @@ class TraceParams(ctypes.Structure):
         ("max_depth", ctypes.c_uint32), ("rr_start", ctypes.c_uint32), ("sky", ctypes.c_float * 3),
         ("tie_mode", ctypes.c_int32), ("kernel", ctypes.c_int32), ("block", ctypes.c_uint32),
         ("stack_depth", ctypes.c_uint32), ("wavefront", ctypes.c_uint32), ("aov_mask", ctypes.c_uint32),
-        ("stats", ctypes.c_uint32),
+        ("stats", ctypes.c_uint32), ("bvh_width", ctypes.c_uint32),
     ]
+
+
+class PresentParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("out_aov", ctypes.c_uint32),
+                ("mode", ctypes.c_uint32)]
+
+
+class CameraController(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_float * 16), ("front", ctypes.c_float * 3), ("pitch", ctypes.c_float),
+                ("yaw", ctypes.c_float), ("last_mouse", ctypes.c_float * 2), ("light_locked", ctypes.c_uint32),
+                ("light_pos", ctypes.c_float * 3)]
+
+
+class InputFrame(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_float), ("keys", ctypes.c_uint32), ("toggle_light", ctypes.c_uint32),
+                ("has_cursor", ctypes.c_uint32), ("cursor_x", ctypes.c_double), ("cursor_y", ctypes.c_double)]
 
 
 class Timings(ctypes.Structure):
@@ -115,6 +135,19 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_trace_batched.argtypes = [vp, vp, ctypes.POINTER(TraceParams), u32, i32, vp]
     lib.tracer_readback_scene.argtypes = [vp, u32, i32, vp, sz]
     lib.tracer_trace_adjoint.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp, vp, vp, vp, vp, vp]
+    lib.tracer_present.argtypes = [vp, vp, vp, u32, u32, i32, ctypes.POINTER(PresentParams), vp, sz, vp]
+    lib.tracer_draw.argtypes = [vp, vp, ctypes.POINTER(TraceParams), ctypes.POINTER(PresentParams), vp, sz, vp]
+    lib.tracer_draw_reset.argtypes = [vp]
+    pc = ctypes.POINTER(CameraController)
+    for fn in ("tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update"):
+        getattr(lib, fn).argtypes = [pc]
+        getattr(lib, fn).restype = None
+    lib.tracer_camera_move.argtypes = [pc, i32, ctypes.c_float]
+    lib.tracer_camera_cursor.argtypes = [pc, ctypes.c_double, ctypes.c_double]
+    lib.tracer_camera_cursor.restype = None
+    lib.tracer_camera_keys.argtypes = [pc, u32, ctypes.c_float]
+    lib.tracer_camera_keys.restype = None
+    lib.tracer_camera_script.argtypes = [pc, ctypes.POINTER(InputFrame), u32, vp]
     if path is None:
         _lib = lib
     return lib
@@ -246,11 +279,13 @@ class Tracer:
 
     @staticmethod
     def params(width, height, spp=4, max_depth=4, rr_start=0, sky=(0.0, 0.0, 0.0), tie_mode=TIES_STRICT,
-               kernel=KERNEL_AUTO, block=0, stack_depth=0, wavefront=0, aovs=(AOV_RGBA8,), stats=False) -> TraceParams:
+               kernel=KERNEL_AUTO, block=0, stack_depth=0, wavefront=0, aovs=(AOV_RGBA8,), stats=False,
+               bvh_width=0) -> TraceParams:
         p = TraceParams()
         p.width, p.height, p.spp, p.max_depth, p.rr_start = width, height, spp, max_depth, rr_start
         p.sky = (ctypes.c_float * 3)(*sky)
         p.tie_mode, p.kernel, p.block, p.stack_depth, p.wavefront = tie_mode, kernel, block, stack_depth, wavefront
+        p.bvh_width = bvh_width
         m = 0
         for a in aovs:
             m |= 1 << a
@@ -348,3 +383,107 @@ class Tracer:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         self._check(self.lib.tracer_device_image(self.h, aov, ctypes.byref(p), ctypes.byref(n)))
         return p.value, n.value
+
+    # ------------------------------------------------------ present pass --
+    @staticmethod
+    def _present_out(width, height, out_aov):
+        if out_aov == AOV_RGBA8:
+            return np.zeros((height, width, 4), np.uint8)
+        return np.zeros((height, width, 4), np.float32)
+
+    def present(self, image0, image1, width: int, height: int, out_aov: int = AOV_RGBA8, out: int | None = None,
+                stream: int | None = None):
+        """tracer_present over two (h, w, 4) images (uint8 RGBA8 or float32
+        RGBA32F numpy arrays, or device addresses with src=(w, h, aov) given
+        as image0=(ptr, w, h, aov)).  Returns the framebuffer (row 0 = top), or
+        None when out is a device address (asynchronous)."""
+        if isinstance(image0, tuple):
+            p0, sw, sh, aov = image0
+            p1 = image1[0]
+            a0, a1 = ctypes.c_void_p(p0), ctypes.c_void_p(p1)
+            keep = ()
+        else:
+            i0, i1 = np.ascontiguousarray(image0), np.ascontiguousarray(image1)
+            assert i0.shape == i1.shape and i0.dtype == i1.dtype
+            sh, sw = i0.shape[:2]
+            aov = AOV_RGBA8 if i0.dtype == np.uint8 else AOV_RGBA32F
+            keep = (i0, i1)
+            a0, a1 = _ptr(i0), _ptr(i1)
+        pp = PresentParams(width, height, out_aov, PRESENT_PINGPONG)
+        nbytes = width * height * (4 if out_aov == AOV_RGBA8 else 16)
+        st = ctypes.c_void_p(stream) if stream else None
+        if out is not None:
+            self._check(self.lib.tracer_present(self.h, a0, a1, sw, sh, aov, ctypes.byref(pp), ctypes.c_void_p(out),
+                                                nbytes, st))
+            return None
+        res = self._present_out(width, height, out_aov)
+        self._check(self.lib.tracer_present(self.h, a0, a1, sw, sh, aov, ctypes.byref(pp), _ptr(res), nbytes, st))
+        del keep
+        return res
+
+    def draw(self, frame: np.ndarray, params: TraceParams, width: int, height: int, mode: int = PRESENT_PINGPONG,
+             out_aov: int = AOV_RGBA8, out: int | None = None, stream: int | None = None):
+        """tracer_draw: trace + present into a width x height framebuffer."""
+        f = np.ascontiguousarray(np.asarray(frame, S.FRAME).reshape(()))
+        pp = PresentParams(width, height, out_aov, mode)
+        nbytes = width * height * (4 if out_aov == AOV_RGBA8 else 16)
+        st = ctypes.c_void_p(stream) if stream else None
+        if out is not None:
+            self._check(self.lib.tracer_draw(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
+                                             ctypes.byref(pp), ctypes.c_void_p(out), nbytes, st))
+            return None
+        res = self._present_out(width, height, out_aov)
+        self._check(self.lib.tracer_draw(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
+                                         ctypes.byref(pp), _ptr(res), nbytes, st))
+        self.width, self.height = params.width, params.height
+        return res
+
+    def draw_reset(self):
+        self._check(self.lib.tracer_draw_reset(self.h))
+
+
+class Camera:
+    """The camera controller of the C ABI (host only; needs the library but
+    no GPU): Camera.cpp plus the main loop's input handling."""
+
+    def __init__(self, startup: bool = False, lib: ctypes.CDLL | None = None):
+        self.lib = lib or load_library()
+        self.c = CameraController()
+        (self.lib.tracer_camera_init_startup if startup else self.lib.tracer_camera_init)(ctypes.byref(self.c))
+
+    def update(self):
+        self.lib.tracer_camera_update(ctypes.byref(self.c))
+
+    def move(self, direction: int, speed: float):
+        r = self.lib.tracer_camera_move(ctypes.byref(self.c), direction, speed)
+        if r != OK:
+            raise TracerError(r, "bad direction")
+
+    def cursor(self, x: float, y: float):
+        self.lib.tracer_camera_cursor(ctypes.byref(self.c), x, y)
+
+    def keys(self, keys: int, dt: float):
+        self.lib.tracer_camera_keys(ctypes.byref(self.c), keys, dt)
+
+    def state(self) -> np.ndarray:
+        """CameraData (16), front (3), pitch, yaw as float32 (21)."""
+        c = self.c
+        return np.array(list(c.data) + list(c.front) + [c.pitch, c.yaw], np.float32)
+
+    def camera(self) -> np.ndarray:
+        return np.frombuffer(bytes(self.c.data), dtype=S.CAMERA).reshape(()).copy()
+
+    def script(self, inputs, frames: np.ndarray | None = None) -> np.ndarray:
+        """inputs: sequence of dicts (dt, keys, toggle_light, cursor=(x, y)
+        or None).  Returns n FrameData records (aspect/seed from frames)."""
+        n = len(inputs)
+        arr = (InputFrame * n)()
+        for i, d in enumerate(inputs):
+            cur = d.get("cursor")
+            arr[i] = InputFrame(d.get("dt", 0.0), d.get("keys", 0), int(d.get("toggle_light", False)),
+                                int(cur is not None), cur[0] if cur else 0.0, cur[1] if cur else 0.0)
+        out = np.zeros(n, S.FRAME) if frames is None else np.ascontiguousarray(np.array(frames, S.FRAME))
+        r = self.lib.tracer_camera_script(ctypes.byref(self.c), arr, n, out.ctypes.data_as(ctypes.c_void_p))
+        if r != OK:
+            raise TracerError(r, "camera script")
+        return out
