@@ -115,6 +115,27 @@ def dist_setup():
     return world, rank, local
 
 
+def rank_seed(seed: float, rank: int) -> float:
+    """Weak scaling: every rank traces its own frame (the reference draws a
+    new seed per frame, GraphicsDevice.cpp:1262)."""
+    return float(seed) + 0.125 * rank
+
+
+def aggregate(world: int, rays: float, seconds: float, device: str = "cuda"):
+    """Whole-job throughput: all ranks' rays over the slowest rank's time.
+    Returns (Mrays/s, max seconds, total rays).  One collective each for the
+    max and the sum; nothing on the data path."""
+    if world == 1:
+        return rays / seconds / 1e6, seconds, rays
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    r = torch.tensor([float(rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(r, op=dist.ReduceOp.SUM)
+    return r.item() / t.item() / 1e6, t.item(), r.item()
+
+
 def cpu_baseline_sample(wl, tri_bvh, seconds_target: float = 15.0):
     """Oracle (CPU port of the shader, same BVH) on a bounded row subset, all
     host threads.  Returns (Mrays/s, threads, description)."""
@@ -191,6 +212,7 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
     best, table = tune.autotune_batched(tr, frames, p_wf, budget_s=40.0)
     for p in p_wf:
         p.block, p.stack_depth, p.wavefront = best["block"], best["stack_depth"], best["wavefront"]
+        p.bvh_width = best["bvh_width"]
     ms_wf = timed(p_wf, True)
     rmse = 0.0
     for k in range(len(wls)):
@@ -333,6 +355,109 @@ def adjoint_section(local: int, steps: int) -> dict:
             "config": {"workload": wl.name, "triangles": len(wl.scene.triangles), "materials": nm}}
 
 
+def small_configs_section(local: int, steps: int, cpu: bool) -> dict:
+    """The reference's own frame (Ref: constant scene, linear scan, reference
+    ties, 1024^2, 4 spp, depth 4) and c0 (64 spheres, median BVH, 512^2,
+    1 spp, depth 2): device-timed Mrays/s of the wavefront and plain kernels,
+    and, with cpu, the oracle's on all host cores (the whole frame)."""
+    import torch
+    from vktrace import abi, configs
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for wl in (configs.ref(), configs.c0()):
+        tr = abi.Tracer(local)
+        tr.upload_scene(wl.scene)
+        res = {}
+        rays = None
+        for name, kern in (("plain", abi.KERNEL_PLAIN), ("wavefront", abi.KERNEL_WAVEFRONT)):
+            p = abi.Tracer.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                                  sky=wl.sky, tie_mode=wl.tie_mode, kernel=kern, stats=rays is None)
+            if rays is None:  # canonical counts from the plain kernel
+                tr.trace(wl.frame, p, sptr)
+                st = tr.stats()
+                rays = st["closest_rays"] + st["shadow_rays"]
+                p.stats = 0
+            for _ in range(3):
+                tr.trace(wl.frame, p, sptr)
+            tr.synchronize()
+            torch.cuda.synchronize()
+            tot = 0.0
+            for _ in range(steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                tr.trace(wl.frame, p, sptr)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                tot += e0.elapsed_time(e1)
+            ms = tot / steps
+            res[name] = {"value": rays / (ms / 1e3) / 1e6, "ms_per_frame": ms}
+        tr.close()
+        res["rays_per_frame"] = rays
+        if cpu:
+            import pyoracle
+            pyoracle.build()
+            prm = pyoracle.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                                  sky=wl.sky, tie_mode=wl.tie_mode, trig_mode=0, threads=os.cpu_count() or 1)
+            tb, sb = None, None
+            if wl.scene.bvh != 0:
+                sb = abi.build_bvh(wl.scene.bvh, wl.scene.spheres, wl.scene.leaf_size, wl.scene.sah_bins)[:2]
+            t0 = time.perf_counter()
+            o = pyoracle.render(wl.scene, wl.frame, prm, tri_bvh=tb, sphere_bvh=sb)
+            dt = time.perf_counter() - t0
+            r = o["stats"]["closest_rays"] + o["stats"]["shadow_rays"]
+            res["cpu_oracle"] = {"value": r / dt / 1e6, "cores": os.cpu_count() or 1, "sample": "whole frame",
+                                 "kind": "port"}
+        out[wl.name] = res
+    return out
+
+
+def present_section(local: int, steps: int) -> dict:
+    """The present pass (Fullscreen.frag) on device images: the reference's
+    sizes (1024^2 RGBA8 images -> 1024x768 framebuffer) and c1's (1920x1080
+    -> 1920x1080).  Per launch: CUDA events around one launch with L2 flushed
+    before it; algorithmic bytes = both source images + the framebuffer."""
+    import numpy as np
+    import torch
+    from vktrace import abi
+    hbm, src = peaks()
+    tr = abi.Tracer(local)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    for name, (sw, sh, w, h) in (("ref_1024_to_1024x768", (1024, 1024, 1024, 768)),
+                                 ("c1_1920x1080", (1920, 1080, 1920, 1080))):
+        a = torch.randint(0, 256, (sh, sw, 4), dtype=torch.uint8, device="cuda", generator=g)
+        b = torch.randint(0, 256, (sh, sw, 4), dtype=torch.uint8, device="cuda", generator=g)
+        fb = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+        call = lambda: tr.present((a.data_ptr(), sw, sh, abi.AOV_RGBA8), (b.data_ptr(),), w, h, abi.AOV_RGBA8,
+                                  out=fb.data_ptr(), stream=sptr)
+        for _ in range(3):
+            call()
+        torch.cuda.synchronize()
+        # the library's CUDA events bracket the kernel alone (the call's host
+        # work -- argument checks, pointer queries -- stays outside)
+        tr.set_profiling(True)
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            call()
+            times.append(tr.timings()["total_ms"])
+        tr.set_profiling(False)
+        ms = float(np.median(times))
+        nbytes = 2 * sw * sh * 4 + w * h * 4
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[name] = {"us_per_launch": ms * 1e3, "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
+                     "frac_of_hbm": gbs / hbm, "peak_source": src}
+    tr.close()
+    return {"kernel": "k_present<uchar4>", "l2": "flushed before each launch", **out}
+
+
 def gd_section(local: int, gd_steps: int, width: int, spp: int, n_tris: int) -> dict:
     """c4: recover perturbed albedos by gradient descent on an L2 image loss
     (1024^2, 64 spp, depth 12, 1M triangles, 1024 materials by default).
@@ -470,7 +595,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     wl = configs.c1(width=args.width, height=args.height, spp=args.spp)
     # weak scaling: each rank its own frame (different seed)
-    wl.frame["seed"] = np.float32(float(wl.frame["seed"]) + 0.125 * rank)
+    wl.frame["seed"] = np.float32(rank_seed(wl.frame["seed"], rank))
     nodes, idx, bvh_depth = abi.build_bvh(2, wl.scene.triangles, leaf_size=4, sah_bins=16)
     tr = abi.Tracer(local)
     tr.upload_scene(wl.scene, tri_bvh=(nodes, idx))
@@ -519,11 +644,8 @@ def run_ours(args):
     clocks = clk.stop()
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = sum(step_ms) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * rays / (ms / 1e3) / 1e6
+    value, max_s, _ = aggregate(world, rays, ms / 1e3)
+    ms = max_s * 1e3
 
     # per-kernel breakdown of one frame (untimed run with CUDA events around
     # every extend and shade launch)
@@ -548,11 +670,7 @@ def run_ours(args):
         tr.trace(wl.frame, p_run)
         tr.readback(abi.AOV_RGBA8, img)
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * rays / e2e_s / 1e6
+    e2e, e2e_s, _ = aggregate(world, rays, e2e_s)
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -602,6 +720,9 @@ def run_ours(args):
             line["batched"] = batched_section(local, max(3, args.steps // 2), 2)
         if world == 1 and not args.no_adjoint:
             line["adjoint"] = adjoint_section(local, max(3, args.steps // 2))
+        if world == 1:
+            line["present"] = present_section(local, 20)
+            line["small_configs"] = small_configs_section(local, 5, not args.no_cpu_baseline)
         print(json.dumps(line), flush=True)
     tr.close()
     if world > 1:

@@ -173,7 +173,8 @@ typedef struct tracer_scene_desc {
 #define TRACER_TIES_REFERENCE 0 /* Tracer.comp:382/:402/:418 scan-order rule; linear scan only */
 #define TRACER_TIES_STRICT 1    /* nearest (t, primitive id) below tmax; required with a BVH */
 
-#define TRACER_KERNEL_AUTO 0      /* = WAVEFRONT */
+#define TRACER_KERNEL_AUTO 0      /* WAVEFRONT for BVH scenes with >= 2^24 pixel x spp x depth, else PLAIN
+                                     (tracer_trace_adjoint: WAVEFRONT from 2^17 pixels) */
 #define TRACER_KERNEL_PLAIN 1     /* one thread per pixel, nested sample/bounce loops */
 #define TRACER_KERNEL_WAVEFRONT 2 /* persistent extend kernel + shade kernel over path queues */
 
@@ -199,8 +200,9 @@ typedef struct tracer_trace_params {
     uint32_t wavefront;     /* wavefront extend kernel: resident CTAs per SM; 0 = occupancy maximum */
     uint32_t aov_mask;      /* bit (1 << TRACER_AOV_*) per image written; 0 = RGBA8 only */
     uint32_t stats;         /* nonzero: count rays, node fetches and primitive tests */
-    uint32_t bvh_width;     /* wavefront traversal: 0 = auto (4-wide nodes when the stack allows), 2 = the
-                               binary BVH, 4 = 4-wide nodes collapsed from it (same boxes, same hits) */
+    uint32_t bvh_width;     /* wavefront traversal: 0 = auto (= 2), 2 = the binary BVH, 4 = 4-wide nodes
+                               collapsed from it (same boxes, same hits; measured slower on sparse
+                               triangle soups, where it tests boxes the binary traversal culls) */
 } tracer_trace_params;
 
 typedef struct tracer_stats {

@@ -781,10 +781,14 @@ static int render(const oracle_scene* sd, const float* frame, const oracle_param
         tid = omp_get_thread_num();
 #endif
         Tracer<T> tr{sc, p.tie, per[tid]};
+        // work items: runs of 64 pixels of one scanline (pixels are independent)
+        const uint32_t run = 64, per_row = (p.width + run - 1) / run;
 #pragma omp for schedule(dynamic, 1)
-        for (long ri = 0; ri < (long)rows.size(); ++ri) {
-            const uint32_t y = rows[ri];
-            for (uint32_t x = 0; x < p.width; ++x) {
+        for (long it = 0; it < (long)rows.size() * (long)per_row; ++it) {
+            const uint32_t y = rows[it / per_row];
+            const uint32_t x0 = (uint32_t)(it % per_row) * run;
+            const uint32_t x1 = x0 + run < p.width ? x0 + run : p.width;
+            for (uint32_t x = x0; x < x1; ++x) {
                 const size_t i = (size_t)y * p.width + x;
                 float rgba[4];
                 uint32_t prim = 0xFFFFFFFFu;

@@ -44,10 +44,17 @@ def _bits(a):
     return fbits(a)
 
 
-def test_batched_equals_single_scene(gpu_tracer):
+@pytest.mark.parametrize("width", [2, 4])
+def test_batched_equals_single_scene(gpu_tracer, width):
+    """Binary and 4-wide traversal of the batch; the single-scene references
+    use the other width, so the two widths are compared too."""
     tr = gpu_tracer
     scenes, frames, params = _batch()
+    for p in params:
+        p.bvh_width = 6 - width
     singles = [_single(tr, sc, fr, p) for sc, fr, p in zip(scenes, frames, params)]
+    for p in params:
+        p.bvh_width = width
     tr.upload_scenes(scenes)
     for use_graph in (False, True, True):  # the second graph run replays the captured graph
         tr.trace_batched(frames, params, use_graph=use_graph)
@@ -116,7 +123,8 @@ def test_timings_after_graph_and_autotune(gpu_tracer):
     best, table = tune.autotune_batched(tr, frames, params, blocks=(64, 128), stacks=(4, 32), wavefronts=(0, 2))
     assert best is not None and best["ms"] > 0
     assert any("skipped" in r for r in table)  # stack 4 is below the BVH depth
-    assert len(table) == 8
+    assert len(table) == 16  # widths 4 and 2
+    assert best["bvh_width"] in (2, 4)
 
 
 def test_batched_argument_errors(gpu_tracer):

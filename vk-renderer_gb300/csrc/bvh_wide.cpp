@@ -27,13 +27,13 @@ bool leaf_code(const tracer_bvh_node& n, int32_t& code)
 
 void set_child(WideNode& w, int k, const tracer_bvh_node& n, int32_t ref)
 {
-    w.lo_x[k] = n.bmin[0];
-    w.lo_y[k] = n.bmin[1];
-    w.lo_z[k] = n.bmin[2];
-    w.hi_x[k] = n.bmax[0];
-    w.hi_y[k] = n.bmax[1];
-    w.hi_z[k] = n.bmax[2];
-    w.child[k] = ref;
+    WideChild& c = w.c[k];
+    for (int a = 0; a < 3; ++a) {
+        c.lo[a] = n.bmin[a];
+        c.hi[a] = n.bmax[a];
+    }
+    c.ref = ref;
+    c.pad = 0;
 }
 
 WideNode empty_node()
@@ -41,10 +41,12 @@ WideNode empty_node()
     WideNode w;
     const float inf = std::numeric_limits<float>::infinity();
     for (int k = 0; k < 4; ++k) {
-        w.lo_x[k] = w.lo_y[k] = w.lo_z[k] = inf;
-        w.hi_x[k] = w.hi_y[k] = w.hi_z[k] = -inf;
-        w.child[k] = 0;
-        w.pad[k] = 0;
+        for (int a = 0; a < 3; ++a) {
+            w.c[k].lo[a] = inf;
+            w.c[k].hi[a] = -inf;
+        }
+        w.c[k].ref = 0;
+        w.c[k].pad = 0;
     }
     return w;
 }

@@ -8,16 +8,20 @@
 
 namespace vkt {
 
-// One node = 128 bytes, read on the device as 8 float4: the boxes of up to
-// four children in structure-of-arrays order, then their references.
-//   child[k] > 0   interior: index of a wide node (the root, 0, is nobody's child)
-//   child[k] < 0   leaf: -1 - ((first << 6) | (count - 1)), primitives
-//                  first .. first + count - 1 of the leaf-ordered arrays
-//   child[k] == 0  empty slot (its box is never tested)
+// One node = 128 bytes, read on the device as 8 float4: for each of up to
+// four children, (box min, reference) (box max, 0).
+//   ref > 0   interior: index of a wide node (the root, 0, is nobody's child)
+//   ref < 0   leaf: -1 - ((first << 6) | (count - 1)), primitives
+//             first .. first + count - 1 of the leaf-ordered arrays
+//   ref == 0  empty slot (its box is never tested)
+struct WideChild {
+    float lo[3];
+    int32_t ref;
+    float hi[3];
+    int32_t pad;
+};
 struct WideNode {
-    float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4];
-    int32_t child[4];
-    int32_t pad[4];
+    WideChild c[4];
 };
 static_assert(sizeof(WideNode) == 128, "wide node is 8 x 16 bytes");
 

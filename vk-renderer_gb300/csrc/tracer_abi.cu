@@ -311,22 +311,24 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     return TRACER_OK;
 }
 
-// Traversal width of the wavefront's extend kernel.  The 4-wide traversal
-// pushes up to three children per level, so it needs 3 x (its depth) stack
-// entries; with bvh_width = 0 it is used when the caller's stack (or, with
-// stack_depth = 0, that bound) allows, else the binary traversal runs.
+// Traversal width of the wavefront's extend kernel: binary unless 4-wide is
+// asked for (bvh_width = 4).  On the soup workloads (100k-1M triangles) the
+// 4-wide traversal measured 8 % slower: visiting a collapsed node tests all
+// four grandchildren's boxes where the binary traversal first culls with the
+// parent's box, and most rays miss most boxes there.  It pushes up to three
+// children per level, so it needs 3 x (its depth) stack entries.
 // stack: in, the binary traversal's stack; out, the stack of the chosen width.
-int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int& wide)
+int pick_width_for(tracer_ctx* c, const tracer_trace_params* p, bool have_wide, uint32_t wide_depth, uint32_t& stack,
+                   int& wide)
 {
     wide = 0;
     if (p->bvh_width != 0 && p->bvh_width != 2 && p->bvh_width != 4)
         return fail(c, TRACER_ERR_INVALID_ARG, "bvh_width %u must be 0, 2 or 4", p->bvh_width);
-    const SceneBuffers& s = c->scene;
-    if (!s.bvh || !s.wide || p->bvh_width == 2) {
+    if (!have_wide || p->bvh_width != 4) {
         if (p->bvh_width == 4) return fail(c, TRACER_ERR_INVALID_ARG, "the scene has no 4-wide BVH");
         return TRACER_OK;
     }
-    const uint32_t need = 3 * s.wide_depth;
+    const uint32_t need = 3 * wide_depth;
     const uint32_t ws = p->stack_depth ? p->stack_depth : need;
     if (ws < need || (size_t)ws * 256 * 8 > 200 * 1024) {
         if (p->bvh_width == 4)
@@ -336,6 +338,12 @@ int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int
     stack = ws;
     wide = 1;
     return TRACER_OK;
+}
+
+int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int& wide)
+{
+    const SceneBuffers& s = c->scene;
+    return pick_width_for(c, p, s.bvh && s.wide, s.wide_depth, stack, wide);
 }
 
 // Builds (or validates) one BVH; returns the leaf-order permutation.
@@ -597,7 +605,15 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
     if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
         return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
-    const int kernel = p->kernel == TRACER_KERNEL_AUTO ? TRACER_KERNEL_WAVEFRONT : p->kernel;
+    // AUTO: the wavefront pays for itself on BVH scenes with enough path
+    // bounces in flight; the plain kernel wins on linear-scan scenes and small
+    // frames (the reference's own 10-primitive frame: 1.6 ms plain against
+    // 2.2 ms wavefront; 512^2 x 1 spp x depth 2: 0.07 against 0.11 ms;
+    // 1920x1080 x 16 spp x depth 8: 225 against 100 ms)
+    const uint64_t bounces = (uint64_t)p->width * p->height * p->spp * p->max_depth;
+    const int kernel = p->kernel != TRACER_KERNEL_AUTO ? p->kernel
+                       : (c->scene.bvh && bounces >= (1ull << 24)) ? TRACER_KERNEL_WAVEFRONT
+                                                                   : TRACER_KERNEL_PLAIN;
     if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
     uint32_t block = p->block ? p->block : 128;
@@ -934,7 +950,9 @@ struct PackedScene {
     std::vector<float4> tri, geo;
     std::vector<uint32_t> sid, emit;
     std::vector<tracer_bvh_node> tnodes, snodes;
-    uint32_t depth = 0;
+    std::vector<WideNode> twide, swide;
+    uint32_t depth = 0, wide_depth = 0;
+    bool wide = false;
     int status = TRACER_OK;
 };
 
@@ -977,6 +995,10 @@ void pack_scene(const tracer_scene_desc& d, PackedScene& out)
         }
     }
     out.depth = td > sd ? td : sd;
+    uint32_t twd = 0, swd = 0;
+    out.wide = collapse_wide4(out.tnodes.data(), (uint32_t)out.tnodes.size(), out.twide, &twd) &&
+               collapse_wide4(out.snodes.data(), (uint32_t)out.snodes.size(), out.swide, &swd);
+    out.wide_depth = twd > swd ? twd : swd;
     out.tri.resize(3 * (size_t)d.num_triangles);
     for (uint32_t k = 0; k < d.num_triangles; ++k) {
         const uint32_t i = tidx[k];
@@ -1047,17 +1069,23 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
             return fail(c, packed[k].status, "scene %u: BVH build or validation failed", k);
 
     // one arena per array kind, scenes back to back
-    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes;
+    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes, twide, swide;
     std::vector<uint32_t> sid, emit;
     struct Off {
-        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit;
+        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit, twide, swide;
     };
     std::vector<Off> off(n);
+    bool wide_all = true;
     for (uint32_t k = 0; k < n; ++k) {
         const tracer_scene_desc& d = descs[k];
         const PackedScene& p = packed[k];
         off[k] = Off{tri.size(), mats.size(), geo.size(), rec.size(), planes.size(), tnodes.size(), snodes.size(),
-                     sid.size(), emit.size()};
+                     sid.size(), emit.size(), twide.size(), swide.size()};
+        wide_all = wide_all && p.wide;
+        const float4* tw = reinterpret_cast<const float4*>(p.twide.data());
+        twide.insert(twide.end(), tw, tw + 8 * p.twide.size());
+        const float4* sw = reinterpret_cast<const float4*>(p.swide.data());
+        swide.insert(swide.end(), sw, sw + 8 * p.swide.size());
         tri.insert(tri.end(), p.tri.begin(), p.tri.end());
         const float4* m = reinterpret_cast<const float4*>(d.materials);
         mats.insert(mats.end(), m, m + 3 * (size_t)d.num_materials);
@@ -1084,10 +1112,14 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
     if (e == cudaSuccess) e = upload(b.sph_nodes, snodes.data(), snodes.size());
     if (e == cudaSuccess) e = upload(b.sph_id, sid.data(), sid.size());
     if (e == cudaSuccess) e = upload(b.emit, emit.data(), emit.size());
+    if (e == cudaSuccess && wide_all) e = upload(b.tri_wide, twide.data(), twide.size());
+    if (e == cudaSuccess && wide_all) e = upload(b.sph_wide, swide.data(), swide.size());
     if (e != cudaSuccess) {
         b.release();
         return cuda_fail(c, e, "batch upload");
     }
+    b.wide = wide_all;
+    b.wide_depth = 0;
     c->batch_scenes.assign(n, DevScene{});
     c->batch_depth.assign(n, 0);
     c->batch_nodes.assign(n, 0);
@@ -1101,7 +1133,10 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
                                       at(b.emit, off[k].emit), at(b.tri_nodes, off[k].tnodes),
                                       at(b.sph_nodes, off[k].snodes), d.num_triangles, d.num_materials, d.num_spheres,
                                       d.num_planes, (uint32_t)p.emit.size(), (uint32_t)p.tnodes.size(),
-                                      (uint32_t)p.snodes.size()};
+                                      (uint32_t)p.snodes.size(),
+                                      wide_all ? at(b.tri_wide, off[k].twide) : nullptr,
+                                      wide_all ? at(b.sph_wide, off[k].swide) : nullptr};
+        b.wide_depth = std::max(b.wide_depth, p.wide_depth);
         c->batch_depth[k] = p.depth;
         c->batch_nodes[k] = (uint32_t)std::max(p.tnodes.size(), p.snodes.size());
         c->batch_emitters = c->batch_emitters || !p.emit.empty();
@@ -1135,10 +1170,15 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         need = std::max(need, c->batch_depth[k]);
         max_nodes = std::max(max_nodes, c->batch_nodes[k]);
     }
-    const uint32_t stack = p0.stack_depth ? p0.stack_depth : need;
+    uint32_t stack = p0.stack_depth ? p0.stack_depth : need;
     if (stack < need) return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
     if ((size_t)stack * 256 * 8 > 200 * 1024)
         return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
+    int wide = 0;
+    if (kernel == TRACER_KERNEL_WAVEFRONT) {
+        int rw = pick_width_for(c, &p0, c->batch.wide, c->batch.wide_depth, stack, wide);
+        if (rw != TRACER_OK) return rw;
+    }
     const uint32_t mask = p0.aov_mask ? p0.aov_mask : (1u << TRACER_AOV_RGBA8);
     const int stats = (p0.stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
     std::vector<size_t> base(n);
@@ -1245,6 +1285,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         wc.multi = 1;
         wc.has_emitters = c->batch_emitters;
         wc.block = block;
+        wc.wide = wide;
         wc.slots = c->batch_slots.p;
         wc.nslots = n;
         if (!use_graph) {
@@ -1261,6 +1302,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
             wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
             // the graph bakes in sizes, launch shapes and buffer addresses
             std::vector<uint64_t> key = {n, total, max_rounds, block, stack, (uint64_t)stats, wc.extend_grid,
+                                         (uint64_t)wide,
                                          (uint64_t)(uintptr_t)c->wf_ray_o.p, (uint64_t)(uintptr_t)c->batch_slots.p,
                                          (uint64_t)(uintptr_t)c->b_rgba8.p, (uint64_t)(uintptr_t)c->b_rgba32f.p,
                                          (uint64_t)(uintptr_t)c->b_hit.p, mask};
@@ -1521,8 +1563,10 @@ int check_present(tracer_ctx* c, const tracer_present_params* pp, size_t out_byt
 
 // The present pass from device images into out (device: asynchronous; host:
 // through the staging buffer, waiting for the result).
+// With profiling on, tracer_last_timings' total_ms then covers the present
+// kernel alone (own_timing) or the whole draw (the trace recorded the start).
 int present_into(tracer_ctx* c, const tracer_present_params* pp, const void* img0, const void* img1, uint32_t sw,
-                 uint32_t sh, int src_float, void* out, cudaStream_t st)
+                 uint32_t sh, int src_float, void* out, cudaStream_t st, bool own_timing)
 {
     const size_t bytes = (size_t)pp->width * pp->height * (pp->out_aov == TRACER_AOV_RGBA8 ? 4 : 16);
     const bool dev_out = is_device_ptr(out);
@@ -1536,7 +1580,9 @@ int present_into(tracer_ctx* c, const tracer_present_params* pp, const void* img
     PresentArgs pa{sw, sh, pp->width, pp->height,
                    pp->out_aov == TRACER_AOV_RGBA8 ? static_cast<uchar4*>(dst) : nullptr,
                    pp->out_aov == TRACER_AOV_RGBA32F ? static_cast<float4*>(dst) : nullptr};
+    if (c->profiling && own_timing) cudaEventRecord(c->prof_begin, st);
     e = launch_present(pa, img0, img1, src_float, st);
+    if (c->profiling) cudaEventRecord(c->prof_end, st);
     c->last_launches += 1;
     if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
     if (e != cudaSuccess) return cuda_fail(c, e, "present launch");
@@ -1594,7 +1640,10 @@ extern "C" int tracer_present(tracer_ctx* c, const void* image0, const void* ima
         src[k] = c->pres_src[k].p;
     }
     c->last_launches = 0;
-    return present_into(c, pp, src[0], src[1], src_width, src_height, src_aov == TRACER_AOV_RGBA32F, out, st);
+    c->last_kernel = 0;
+    c->last_rounds = 0;
+    c->last_prof_rounds = 0;
+    return present_into(c, pp, src[0], src[1], src_width, src_height, src_aov == TRACER_AOV_RGBA32F, out, st, true);
 }
 
 extern "C" int tracer_draw(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params* p,
@@ -1627,7 +1676,7 @@ extern "C" int tracer_draw(tracer_ctx* c, const tracer_frame* f, const tracer_tr
         const int s = (int)(c->draw_frame & 1);
         e = cudaMemcpyAsync(c->slot[s].p, c->rgba8.p, npx * sizeof(uchar4), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return cuda_fail(c, e, "frame slot copy");
-        r = present_into(c, pp, c->slot[0].p, c->slot[1].p, q.width, q.height, 0, out, st);
+        r = present_into(c, pp, c->slot[0].p, c->slot[1].p, q.width, q.height, 0, out, st, false);
     } else {
         // the camera's four vectors, bit for bit (not its padding lanes)
         const tracer_camera &ca = c->acc_frame.camera, &cb = f->camera;
@@ -1659,7 +1708,7 @@ extern "C" int tracer_draw(tracer_ctx* c, const tracer_frame* f, const tracer_tr
                               st);
         c->last_launches += 1;
         if (e != cudaSuccess) return cuda_fail(c, e, "accumulate launch");
-        r = present_into(c, pp, c->acc_disp[cur].p, c->acc_disp[cur ^ 1].p, q.width, q.height, 1, out, st);
+        r = present_into(c, pp, c->acc_disp[cur].p, c->acc_disp[cur ^ 1].p, q.width, q.height, 1, out, st, false);
     }
     if (r == TRACER_OK) ++c->draw_frame;
     return r;

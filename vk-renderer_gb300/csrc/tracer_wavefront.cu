@@ -180,18 +180,24 @@ __device__ __forceinline__ void order2(float& ta, int& ra, float& tb, int& rb)
 template <bool STATS>
 __device__ __forceinline__ void visit_wide(Lane& L, int w, const Stack& stk, int* status, Counters& cnt)
 {
+    // node = four (box min, reference) (box max, 0) records
     const float4* n = L.nodes + 8 * (size_t)w;
-    const float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
-    const float4 lz = __ldg(n + 4), hz = __ldg(n + 5);
-    const int4 ch = __ldg(reinterpret_cast<const int4*>(n + 6));
     const float INF = __int_as_float(0x7f800000);
     float t0, t1, t2, t3;
-    int r0 = ch.x, r1 = ch.y, r2 = ch.z, r3 = ch.w;
-    if (STATS) cnt.c[C_NODES] += (r0 != 0) + (r1 != 0) + (r2 != 0) + (r3 != 0);
-    if (!(r0 != 0 && box_hit_s(L.br, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, L.h.t, t0))) { t0 = INF; r0 = 0; }
-    if (!(r1 != 0 && box_hit_s(L.br, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, L.h.t, t1))) { t1 = INF; r1 = 0; }
-    if (!(r2 != 0 && box_hit_s(L.br, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, L.h.t, t2))) { t2 = INF; r2 = 0; }
-    if (!(r3 != 0 && box_hit_s(L.br, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, L.h.t, t3))) { t3 = INF; r3 = 0; }
+    int r0, r1, r2, r3;
+    auto child = [&](int k, float& t, int& r) {
+        const float4 lo = __ldg(n + 2 * k), hi = __ldg(n + 2 * k + 1);
+        r = __float_as_int(lo.w);
+        if (STATS) cnt.c[C_NODES] += r != 0;
+        if (!(r != 0 && box_hit(L.br, lo, hi, L.h.t, t))) {
+            t = INF;
+            r = 0;
+        }
+    };
+    child(0, t0, r0);
+    child(1, t1, r1);
+    child(2, t2, r2);
+    child(3, t3, r3);
     // sorting network: ascending distance (misses last)
     order2(t0, r0, t1, r1);
     order2(t2, r2, t3, r3);
@@ -230,10 +236,9 @@ __device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters
     }
 }
 
-// 1024 resident threads per SM for the binary traversal (64 registers); the
-// 4-wide node visit holds four boxes at once and gets 80 (768 threads).
+// 1024 resident threads per SM (64 registers).
 template <int TIE, bool STATS, bool MULTI, int BLOCK, bool WIDE>
-__global__ void __launch_bounds__(BLOCK, (WIDE ? 768 : 1024) / BLOCK)
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     wf_extend_bvh(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
     extern __shared__ int smem[];

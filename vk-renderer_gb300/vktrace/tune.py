@@ -1,6 +1,7 @@
 """Autotuner for the wavefront launch shape.
 
-Sweeps the extend kernel's block size, the traversal stack depth and the
+Sweeps the extend kernel's block size, the traversal stack depth (0 = the
+bound the BVH needs), the traversal width (4-wide or binary nodes) and the
 "wavefront size" (resident extend CTAs per SM, i.e. how many rays are in
 flight at once), timing each candidate on the device with CUDA events
 (tracer_last_timings), and returns the fastest.  Candidates the library
@@ -15,26 +16,28 @@ import time
 from . import abi
 
 
-def _set(params, block, stack, wave):
+def _set(params, block, stack, wave, width):
     for p in params:
-        p.block, p.stack_depth, p.wavefront = block, stack, wave
+        p.block, p.stack_depth, p.wavefront, p.bvh_width = block, stack, wave, width
 
 
-def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stacks=(16, 32, 64),
-                     wavefronts=(0, 6, 4), reps: int = 1, use_graph: bool = True, budget_s: float = 60.0):
-    """Returns (best, table): best = dict(block, stack_depth, wavefront, ms);
-    table = one dict per candidate (ms or skipped reason)."""
+def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stacks=(0, 16, 32, 64),
+                     wavefronts=(0, 6, 4), widths=(4, 2), reps: int = 1, use_graph: bool = True,
+                     budget_s: float = 60.0):
+    """Returns (best, table): best = dict(block, stack_depth, wavefront,
+    bvh_width, ms); table = one dict per candidate (ms or skipped reason)."""
     table = []
     best = None
     t_start = time.perf_counter()
-    saved = [(p.block, p.stack_depth, p.wavefront) for p in params]
+    saved = [(p.block, p.stack_depth, p.wavefront, p.bvh_width) for p in params]
     tr.set_profiling(True)
     try:
-        for block, stack, wave in itertools.product(blocks, stacks, wavefronts):
+        for width, block, stack, wave in itertools.product(widths, blocks, stacks, wavefronts):
+            cand = {"block": block, "stack_depth": stack, "wavefront": wave, "bvh_width": width}
             if time.perf_counter() - t_start > budget_s:
-                table.append({"block": block, "stack_depth": stack, "wavefront": wave, "skipped": "time budget"})
+                table.append(dict(cand, skipped="time budget"))
                 continue
-            _set(params, block, stack, wave)
+            _set(params, block, stack, wave, width)
             try:
                 tr.trace_batched(frames, params, use_graph=use_graph)  # first run: graph capture, caches warm
                 tr.synchronize()
@@ -44,16 +47,16 @@ def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stac
                     times.append(tr.timings()["total_ms"])
                 ms = sorted(times)[len(times) // 2]
             except abi.TracerError as e:
-                table.append({"block": block, "stack_depth": stack, "wavefront": wave, "skipped": str(e)})
+                table.append(dict(cand, skipped=str(e)))
                 continue
-            row = {"block": block, "stack_depth": stack, "wavefront": wave, "ms": ms}
+            row = dict(cand, ms=ms)
             table.append(row)
             if best is None or ms < best["ms"]:
                 best = dict(row)
     finally:
         tr.set_profiling(False)
-        for p, (b, s, w) in zip(params, saved):
-            p.block, p.stack_depth, p.wavefront = b, s, w
+        for p, (b, s, w, wd) in zip(params, saved):
+            p.block, p.stack_depth, p.wavefront, p.bvh_width = b, s, w, wd
     return best, table
 
 
