@@ -362,6 +362,7 @@ def small_configs_section(local: int, steps: int, cpu: bool) -> dict:
     and, with cpu, the oracle's on all host cores (the whole frame)."""
     import torch
     from vktrace import abi, configs
+    from vktrace import scene as S
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -411,6 +412,40 @@ def small_configs_section(local: int, steps: int, cpu: bool) -> dict:
             res["cpu_oracle"] = {"value": r / dt / 1e6, "cores": os.cpu_count() or 1, "sample": "whole frame",
                                  "kind": "port"}
         out[wl.name] = res
+    # the legacy Whitted shader (Raytracer.comp) on its own scene, the
+    # start-up frame at the reference's 1024^2
+    tr = abi.Tracer(local)
+    fr = S.reference_frame(0.5)
+    p = abi.Tracer.params(1024, 1024, stats=True)
+    tr.trace_whitted(fr, p, sptr)
+    st = tr.stats()
+    rays = st["closest_rays"] + st["shadow_rays"]
+    p.stats = 0
+    for _ in range(3):
+        tr.trace_whitted(fr, p, sptr)
+    tr.synchronize()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        tr.trace_whitted(fr, p, sptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    tr.close()
+    ms = tot / steps
+    res = {"gpu": {"value": rays / (ms / 1e3) / 1e6, "ms_per_frame": ms}, "rays_per_frame": rays}
+    if cpu:
+        import pyoracle
+        t0 = time.perf_counter()
+        o = pyoracle.whitted(fr, 1024, 1024)
+        dt = time.perf_counter() - t0
+        r = o["stats"]["closest_rays"] + o["stats"]["shadow_rays"]
+        res["cpu_oracle"] = {"value": r / dt / 1e6, "cores": os.cpu_count() or 1, "sample": "whole frame",
+                             "kind": "port"}
+    out["whitted-raytracer.comp-1024x1024"] = res
     return out
 
 
@@ -746,6 +781,7 @@ def main():
     ap.add_argument("--gd-steps", type=int, default=0,
                     help="run only the gradient-descent workload (c4 shape) for this many steps")
     ap.add_argument("--gd-tris", type=int, default=1_000_000)
+    ap.add_argument("--present-only", action="store_true", help="time the present pass alone (--steps launches)")
     # smaller variants of the workload (profiling captures); defaults = c1
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
@@ -759,6 +795,10 @@ def main():
         w = args.width if args.width != 1920 else 1024
         spp = args.spp if args.spp != 16 else 64
         print(json.dumps(gd_section(dist_setup()[2], args.gd_steps, w, spp, args.gd_tris)), flush=True)
+    elif args.present_only:
+        import torch
+        torch.cuda.set_device(dist_setup()[2])
+        print(json.dumps(present_section(dist_setup()[2], args.steps)), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -393,6 +393,18 @@ int tracer_draw(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_p
  * frame 0. */
 int tracer_draw_reset(tracer_ctx* ctx);
 
+/* ------------------------------------------------------------ legacy Whitted shader
+ * Assets/Raytracer.comp, the reference's second compute shader, which its
+ * program does not load (it dispatches Tracer.comp): a Whitted ray tracer over
+ * its own constant scene (one triangle, two spheres, five planes), one point
+ * light at frame->light_pos with a shadow ray, two mirror bounces.  Reads
+ * frame's aspect_ratio, light_pos and camera (the shader's push-constant
+ * offsets equal FrameData's) and params' width, height, aov_mask (RGBA8,
+ * RGBA32F, STATS) and stats; needs no uploaded scene.  Output as for
+ * tracer_trace (tracer_readback). */
+int tracer_trace_whitted(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
+                         void* cuda_stream);
+
 /* ------------------------------------------------------------ camera
  * The reference's camera controller (Camera, Source/Camera.cpp:5-64) with the
  * input handling of its main loop (Source/Main.cpp:23-83), for scripted

@@ -63,6 +63,11 @@ void oracle_present(const void* image0, const void* image1, int src_is_float, ui
 void oracle_accumulate(const float* linear_rgba, float* sum_rgba, uint32_t n_pixels, uint32_t n,
                        float* display_rgba);
 
+/* whitted_oracle.cpp: the legacy Whitted shader (Assets/Raytracer.comp) over
+ * its constant scene; frame: the 96-byte FrameData. */
+void oracle_whitted(const float* frame96, uint32_t width, uint32_t height, float* rgba32f, uint8_t* rgba8,
+                    oracle_stats* stats);
+
 typedef struct oracle_camera_ctl {
     float cam[16];        /* CameraData: pos, dir, right, up (16-byte lanes) */
     float front[3];

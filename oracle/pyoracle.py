@@ -95,6 +95,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_present.restype = None
         L.oracle_accumulate.argtypes = [vp, vp, u32, u32, vp]
         L.oracle_accumulate.restype = None
+        L.oracle_whitted.argtypes = [vp, u32, u32, vp, vp, ctypes.POINTER(OStats)]
+        L.oracle_whitted.restype = None
         pc = ctypes.POINTER(OCameraCtl)
         for fn, args in (("oracle_camera_init", [pc]), ("oracle_camera_update", [pc]),
                          ("oracle_camera_move", [pc, i32, f32]),
@@ -341,3 +343,27 @@ def ref_camera_ops(ops, args):
     out = np.zeros((len(op), 21), np.float32)
     L.ref_camera_ops(len(op), _p(op), _p(ar), _p(out))
     return out
+
+
+# ---------------------------------------------------- legacy Whitted shader --
+def whitted(frame, width, height):
+    """Assets/Raytracer.comp restated (oracle/whitted_oracle.cpp): returns
+    dict(rgba32f, rgba8, stats)."""
+    f = np.ascontiguousarray(frame).reshape(())
+    rgba = np.zeros((height, width, 4), np.float32)
+    u8 = np.zeros((height, width, 4), np.uint8)
+    st = OStats()
+    lib().oracle_whitted(f.ctypes.data_as(ctypes.c_void_p), width, height, _p(rgba), _p(u8), ctypes.byref(st))
+    return {"rgba32f": rgba, "rgba8": u8, "stats": {k: int(getattr(st, k)) for k in STATS_FIELDS}}
+
+
+def ref_whitted(frame, width, height):
+    """The reference's Raytracer.comp compiled for the host (oracle/_ref)."""
+    L = ctypes.CDLL(os.path.join(REF_DIR, "libref_whitted.so"))
+    L.ref_whitted_render.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.ref_whitted_render.restype = None
+    f = np.ascontiguousarray(frame).reshape(())
+    rgba = np.zeros((height, width, 4), np.float32)
+    u8 = np.zeros((height, width, 4), np.uint8)
+    L.ref_whitted_render(f.ctypes.data_as(ctypes.c_void_p), width, height, _p(rgba), _p(u8))
+    return rgba, u8

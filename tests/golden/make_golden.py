@@ -19,9 +19,10 @@ those libraries and records their outputs:
   ref_present.npz    the present pass (Assets/Fullscreen.frag) on random image
                      pairs, RGBA8 and float
   ref_camera.npz     Camera.cpp operations from the default camera
+  ref_whitted.npz    the legacy Assets/Raytracer.comp on two frames
 
 Run here (needs the reference tree):  python tests/golden/make_golden.py
-(--present: only the last two)
+(--present: only the last three)
 """
 from __future__ import annotations
 
@@ -98,6 +99,21 @@ def present_and_camera():
     states = pyoracle.ref_camera_ops(ops, args)
     np.savez(os.path.join(HERE, "ref_camera.npz"), ops=np.array(ops, np.int32),
              args=np.array(args, np.float32).reshape(-1, 2), states=states)
+
+    # the legacy Whitted shader (Assets/Raytracer.comp): the start-up frame and
+    # a second camera/light, small sizes in full, 1024^2 as hashes
+    fr2 = S.frame(S.look_at((0.0, 40.0, -60.0), (0.0, 20.0, 30.0), 60.0), 4 / 3, 0.2, (10.0, 60.0, 10.0))
+    frames = [S.reference_frame(0.5), fr2]
+    # frames as raw 96-byte records (24 floats): a stacked structured array
+    # would lose its field offsets in the .npz
+    wh = {"frames": np.stack([np.frombuffer(f.tobytes(), np.float32) for f in frames])}
+    for k, fr in enumerate(frames):
+        for w, h in ((64, 48), (97, 61)):
+            img, u8 = pyoracle.ref_whitted(fr, w, h)
+            wh[f"f{k}_{w}x{h}_rgba32f"], wh[f"f{k}_{w}x{h}_rgba8"] = img, u8
+        img, u8 = pyoracle.ref_whitted(fr, 1024, 1024)
+        wh[f"f{k}_1024_sha_rgba32f"], wh[f"f{k}_1024_sha_rgba8"] = np.array(sha(img)), np.array(sha(u8))
+    np.savez_compressed(os.path.join(HERE, "ref_whitted.npz"), **wh)
 
 
 def main():

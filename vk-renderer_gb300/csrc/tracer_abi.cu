@@ -1729,3 +1729,58 @@ extern "C" int tracer_draw_reset(tracer_ctx* c)
     c->acc_n = 0;
     return TRACER_OK;
 }
+
+// ------------------------------------------------------------ legacy Whitted
+extern "C" int tracer_trace_whitted(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params* p,
+                                    void* cuda_stream)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (!f || !p) return fail(c, TRACER_ERR_INVALID_ARG, "null frame or params");
+    if (p->width == 0 || p->height == 0 || p->width > 32768 || p->height > 32768)
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "image size %ux%u not supported", p->width, p->height);
+    const uint32_t mask = p->aov_mask ? p->aov_mask : (1u << TRACER_AOV_RGBA8);
+    if (mask & ~((1u << TRACER_AOV_RGBA8) | (1u << TRACER_AOV_RGBA32F) | (1u << TRACER_AOV_STATS)))
+        return fail(c, TRACER_ERR_NO_SUITABLE_SURFACE, "the Whitted shader writes RGBA8, RGBA32F and STATS only");
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    cudaSetDevice(c->device);
+    const size_t npx = (size_t)p->width * p->height;
+    cudaError_t e = cudaSuccess;
+    if (mask & (1u << TRACER_AOV_RGBA8)) e = dalloc(c->rgba8, npx);
+    if (e == cudaSuccess && (mask & (1u << TRACER_AOV_RGBA32F))) e = dalloc(c->rgba32f, npx);
+    if (e != cudaSuccess) return cuda_fail(c, e, "image allocation");
+    TraceArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.fr.aspect = f->aspect_ratio;
+    a.fr.seed = f->seed;
+    a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
+    a.fr.cdir = V3{f->camera.dir[0], f->camera.dir[1], f->camera.dir[2]};
+    a.fr.cright = V3{f->camera.right[0], f->camera.right[1], f->camera.right[2]};
+    a.fr.cup = V3{f->camera.up[0], f->camera.up[1], f->camera.up[2]};
+    a.fr.light = V3{f->light_pos[0], f->light_pos[1], f->light_pos[2]};
+    a.width = p->width;
+    a.height = p->height;
+    a.rgba8 = (mask & (1u << TRACER_AOV_RGBA8)) ? c->rgba8.p : nullptr;
+    a.rgba32f = (mask & (1u << TRACER_AOV_RGBA32F)) ? c->rgba32f.p : nullptr;
+    a.stats = c->stats.p;
+    a.status = c->status.p;
+    const int stats = (p->stats || (mask & (1u << TRACER_AOV_STATS))) ? 1 : 0;
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->stream;
+    e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "trace set-up");
+    c->width = p->width;
+    c->height = p->height;
+    c->last_mask = mask | (stats ? (1u << TRACER_AOV_STATS) : 0u);
+    c->last_kernel = 0;
+    c->last_rounds = 0;
+    c->last_prof_rounds = 0;
+    c->last_launches = 1;
+    if (c->profiling) cudaEventRecord(c->prof_begin, st);
+    e = launch_whitted(a, stats, st);
+    if (c->profiling) cudaEventRecord(c->prof_end, st);
+    if (e == cudaSuccess) e = cudaEventRecord(c->done, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "Whitted launch");
+    c->pending = true;
+    return TRACER_OK;
+}

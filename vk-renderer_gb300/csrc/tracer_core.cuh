@@ -11,6 +11,7 @@ namespace vkt {
 struct FrameArgs {
     float aspect, seed;
     V3 cpos, cdir, cright, cup;
+    V3 light;  // FrameData::light_pos (read only by the legacy Whitted shader)
 };
 
 struct TraceArgs {

@@ -19,6 +19,9 @@ struct LaunchConfig {
 };
 
 cudaError_t launch_plain(const TraceArgs& a, const LaunchConfig& lc, cudaStream_t s);
+// The legacy Whitted shader over its constant scene (uses a.fr, a.width,
+// a.height, a.rgba8 / a.rgba32f, a.stats).
+cudaError_t launch_whitted(const TraceArgs& a, int stats, cudaStream_t s);
 cudaError_t launch_adjoint(const TraceArgs& a, const float4* dldi, const float4* linear, double* grad, uint32_t nm,
                            int tie, int bvh, cudaStream_t s);
 // out[i] = (float)g[i], i < n

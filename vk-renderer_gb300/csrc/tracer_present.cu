@@ -31,21 +31,27 @@
 
 namespace vkt {
 
-__device__ __forceinline__ V3 texel(const uchar4* im, uint32_t w, uint32_t h, int i, int j)
+// c / 255 for the 256 UNORM8 codes (IEEE division, computed once per block
+// into shared memory: the same values as dividing per texel)
+struct Unorm {
+    const float* lut;
+};
+
+__device__ __forceinline__ V3 texel(const uchar4* im, uint32_t w, uint32_t h, int i, int j, Unorm u)
 {
     if (i < 0 || j < 0 || i >= (int)w || j >= (int)h) return splat(0.0f);
     const uchar4 c = __ldg(im + (size_t)j * w + i);
-    return v3((float)c.x / 255.0f, (float)c.y / 255.0f, (float)c.z / 255.0f);
+    return v3(u.lut[c.x], u.lut[c.y], u.lut[c.z]);
 }
 
-__device__ __forceinline__ V3 texel(const float4* im, uint32_t w, uint32_t h, int i, int j)
+__device__ __forceinline__ V3 texel(const float4* im, uint32_t w, uint32_t h, int i, int j, Unorm)
 {
     if (i < 0 || j < 0 || i >= (int)w || j >= (int)h) return splat(0.0f);
     return v3(__ldg(im + (size_t)j * w + i));
 }
 
 template <class T>
-__device__ __forceinline__ V3 bilinear(const T* im, uint32_t w, uint32_t h, float s, float t)
+__device__ __forceinline__ V3 bilinear(const T* im, uint32_t w, uint32_t h, float s, float t, Unorm un)
 {
     const float u = s * (float)w - 0.5f;
     const float v = t * (float)h - 0.5f;
@@ -56,29 +62,36 @@ __device__ __forceinline__ V3 bilinear(const T* im, uint32_t w, uint32_t h, floa
     const float w10 = al * (1.0f - be);
     const float w01 = (1.0f - al) * be;
     const float w11 = al * be;
-    const V3 a = texel(im, w, h, i0, j0), b = texel(im, w, h, i0 + 1, j0);
-    const V3 c = texel(im, w, h, i0, j0 + 1), d = texel(im, w, h, i0 + 1, j0 + 1);
+    const V3 a = texel(im, w, h, i0, j0, un), b = texel(im, w, h, i0 + 1, j0, un);
+    const V3 c = texel(im, w, h, i0, j0 + 1, un), d = texel(im, w, h, i0 + 1, j0 + 1, un);
     return ((a * w00 + b * w10) + c * w01) + d * w11;
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) k_present(PresentArgs p, const T* __restrict__ img0, const T* __restrict__ img1)
 {
+    __shared__ float lut[256];
+    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = (float)i / 255.0f;
+    __syncthreads();
+    const Unorm un{lut};
     const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31);
     const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= p.width || y >= p.height) return;
     const float s = ((float)x + 0.5f) / (float)p.width;
     const float t = 1.0f - ((float)y + 0.5f) / (float)p.height;
     const float inv = 1.0f / 2048.0f;  // Fullscreen.frag:12, half a texel of the reference's 1024^2 image
-    const V3 c0 = bilinear(img0, p.src_w, p.src_h, s, t);
-    const V3 c1 = bilinear(img1, p.src_w, p.src_h, s, t);
-    const V3 n = bilinear(img0, p.src_w, p.src_h, s + 0.0f * inv, t + 1.0f * inv);
-    const V3 so = bilinear(img0, p.src_w, p.src_h, s + 0.0f * inv, t + -1.0f * inv);
-    const V3 e = bilinear(img0, p.src_w, p.src_h, s + 1.0f * inv, t + 0.0f * inv);
-    const V3 w = bilinear(img0, p.src_w, p.src_h, s + -1.0f * inv, t + 0.0f * inv);
+    const V3 c0 = bilinear(img0, p.src_w, p.src_h, s, t, un);
+    const V3 c1 = bilinear(img1, p.src_w, p.src_h, s, t, un);
     const V3 d = c0 - c1;
     const float vT = dot(d, d);
-    const V3 f = vT > 0.0005f ? (((n + so) + e) + w) / 4.0f : c0;
+    V3 f = c0;
+    if (vT > 0.0005f) {  // the four taps are only read where the variance test fires
+        const V3 n = bilinear(img0, p.src_w, p.src_h, s + 0.0f * inv, t + 1.0f * inv, un);
+        const V3 so = bilinear(img0, p.src_w, p.src_h, s + 0.0f * inv, t + -1.0f * inv, un);
+        const V3 e = bilinear(img0, p.src_w, p.src_h, s + 1.0f * inv, t + 0.0f * inv, un);
+        const V3 w = bilinear(img0, p.src_w, p.src_h, s + -1.0f * inv, t + 0.0f * inv, un);
+        f = (((n + so) + e) + w) / 4.0f;
+    }
     const size_t o = (size_t)y * p.width + x;
     if (p.out8) p.out8[o] = make_uchar4(unorm8(f.x), unorm8(f.y), unorm8(f.z), 255);
     if (p.out32) p.out32[o] = make_float4(f.x, f.y, f.z, 1.0f);

@@ -41,7 +41,7 @@ EXPORTED_SYMBOLS = [
     "tracer_last_timings", "tracer_trace_noalloc", "tracer_upload_scenes", "tracer_trace_batched",
     "tracer_readback_scene", "tracer_trace_adjoint", "tracer_present", "tracer_draw", "tracer_draw_reset",
     "tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update", "tracer_camera_move",
-    "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script",
+    "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script", "tracer_trace_whitted",
 ]
 PRESENT_PINGPONG, PRESENT_ACCUMULATE = 0, 1
 KEY_W, KEY_S, KEY_A, KEY_D, KEY_R, KEY_F = 1, 2, 4, 8, 16, 32
@@ -138,6 +138,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_present.argtypes = [vp, vp, vp, u32, u32, i32, ctypes.POINTER(PresentParams), vp, sz, vp]
     lib.tracer_draw.argtypes = [vp, vp, ctypes.POINTER(TraceParams), ctypes.POINTER(PresentParams), vp, sz, vp]
     lib.tracer_draw_reset.argtypes = [vp]
+    lib.tracer_trace_whitted.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp]
     pc = ctypes.POINTER(CameraController)
     for fn in ("tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update"):
         getattr(lib, fn).argtypes = [pc]
@@ -383,6 +384,13 @@ class Tracer:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         self._check(self.lib.tracer_device_image(self.h, aov, ctypes.byref(p), ctypes.byref(n)))
         return p.value, n.value
+
+    def trace_whitted(self, frame: np.ndarray, params: TraceParams, stream: int | None = None):
+        """tracer_trace_whitted: the legacy Raytracer.comp over its own scene."""
+        f = np.ascontiguousarray(np.asarray(frame, S.FRAME).reshape(()))
+        self._check(self.lib.tracer_trace_whitted(self.h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(params),
+                                                  ctypes.c_void_p(stream) if stream else None))
+        self.width, self.height = params.width, params.height
 
     # ------------------------------------------------------ present pass --
     @staticmethod
