@@ -1,0 +1,65 @@
+"""Failure paths that need a GPU but fault nothing: a bounded wait that runs
+out returns TRACER_ERR_TIMEOUT and leaves the context usable (the kernel
+itself finishes normally); argument checks refuse bad launches before any
+kernel runs."""
+import numpy as np
+import pytest
+
+from gpu_cases import soup_scene
+from vktrace import abi, configs
+from vktrace import scene as S
+
+pytestmark = pytest.mark.gpu
+
+
+def test_bounded_wait_times_out_then_recovers():
+    """A 1 ms wait on a ~200 ms frame (the plain kernel: one launch, so the
+    trace call itself never waits): the readback reports a timeout instead of
+    blocking; with the default limit back, the same frame completes and
+    matches a trace that was never interrupted."""
+    wl = configs.c1()
+    with abi.Tracer(0) as tr:
+        tr.upload_scene(wl.scene)
+        p = abi.Tracer.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
+                              sky=wl.sky, kernel=abi.KERNEL_PLAIN, aovs=(abi.AOV_RGBA8,))
+        tr.trace(wl.frame, p)
+        tr.synchronize()
+        ref = tr.readback(abi.AOV_RGBA8)
+        tr.set_timeout(1)
+        tr.trace(wl.frame, p)
+        with pytest.raises(abi.TracerError) as e:
+            tr.readback(abi.AOV_RGBA8)
+        assert e.value.status == abi.ERR_TIMEOUT
+        tr.set_timeout(60000)
+        tr.synchronize()
+        again = tr.readback(abi.AOV_RGBA8)
+        assert np.array_equal(again, ref)
+
+
+def test_refused_launches_leave_context_usable(gpu_tracer):
+    tr = gpu_tracer
+    sc = soup_scene(9, 800)
+    tr.upload_scene(sc)
+    fr = S.frame(S.look_at((0.0, 0.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.3)
+    bad = [
+        abi.Tracer.params(0, 16),                                   # empty image
+        abi.Tracer.params(16, 16, spp=0),                           # no samples
+        abi.Tracer.params(16, 16, tie_mode=abi.TIES_REFERENCE),     # reference ties need a linear scan
+        abi.Tracer.params(16, 16, kernel=7),                        # unknown kernel
+        abi.Tracer.params(16, 16, kernel=abi.KERNEL_WAVEFRONT, block=96),
+        abi.Tracer.params(16, 16, stack_depth=1),                   # below the BVH depth
+        abi.Tracer.params(16, 16, aovs=(9,)),                       # unknown AOV
+    ]
+    for p in bad:
+        with pytest.raises(abi.TracerError):
+            tr.trace(fr, p)
+    p = abi.Tracer.params(16, 16, spp=2, max_depth=3)
+    tr.trace(fr, p)
+    assert tr.readback(abi.AOV_RGBA8).shape == (16, 16, 4)
+
+
+def test_no_scene():
+    with abi.Tracer(0) as tr:
+        with pytest.raises(abi.TracerError) as e:
+            tr.trace(S.reference_frame(0.5), abi.Tracer.params(8, 8))
+        assert e.value.status == abi.ERR_NO_SCENE

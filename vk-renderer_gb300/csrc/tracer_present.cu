@@ -20,9 +20,12 @@
 // single-precision operation in the order written (--fmad=false), so the
 // output is bit-identical to the oracle's.
 //
-// Both kernels stream their images once; taps of neighbouring threads share
-// texels through L1, so the DRAM traffic is the two source images plus the
-// output (HBM-bound; a few microseconds at 1024 x 1024).
+// k_present reads each source texel from DRAM once (taps of neighbouring
+// threads share texels through L1) and is bound by instruction issue: six
+// bilinear taps of twelve texel channels each.  Hence the UNORM conversion
+// and the floor / float-to-int steps below avoid the conversion unit (its
+// throughput is an eighth of the FMA pipe's), and the four neighbour taps are
+// only evaluated where the variance test needs them.
 
 #include <cuda_runtime.h>
 
@@ -31,65 +34,96 @@
 
 namespace vkt {
 
-// c / 255 for the 256 UNORM8 codes (IEEE division, computed once per block
-// into shared memory: the same values as dividing per texel)
-struct Unorm {
-    const float* lut;
-};
-
-__device__ __forceinline__ V3 texel(const uchar4* im, uint32_t w, uint32_t h, int i, int j, Unorm u)
+// c / 255, correctly rounded, for the UNORM8 codes c = 0..255: q = c * (1/255)
+// and one residual correction (Markstein's method: r = c - 255 q exactly by
+// fma, q + r / 255 ~ q + r * (1/255)).  Equal to the IEEE quotient for all 256
+// codes (checked exhaustively with exact rational arithmetic), three
+// instructions instead of a division.  The byte becomes a float without the
+// conversion unit: one byte permute builds the float 2^23 + c, and
+// subtracting 2^23 leaves c exactly.
+template <int K>
+__device__ __forceinline__ float unorm_to_float(uint32_t word)
 {
-    if (i < 0 || j < 0 || i >= (int)w || j >= (int)h) return splat(0.0f);
-    const uchar4 c = __ldg(im + (size_t)j * w + i);
-    return v3(u.lut[c.x], u.lut[c.y], u.lut[c.z]);
+    const float fc = __uint_as_float(__byte_perm(word, 0x4B000000u, K | (4 << 4) | (4 << 8) | (7 << 12))) - 8388608.0f;
+    const float inv = 1.0f / 255.0f;
+    const float q = fc * inv;
+    const float r = __fmaf_rn(-q, 255.0f, fc);
+    return __fmaf_rn(r, inv, q);
 }
 
-__device__ __forceinline__ V3 texel(const float4* im, uint32_t w, uint32_t h, int i, int j, Unorm)
+__device__ __forceinline__ V3 texel_at(const uchar4* im, size_t k)
 {
-    if (i < 0 || j < 0 || i >= (int)w || j >= (int)h) return splat(0.0f);
-    return v3(__ldg(im + (size_t)j * w + i));
+    const uint32_t c = __ldg(reinterpret_cast<const uint32_t*>(im) + k);  // R in the low byte
+    return v3(unorm_to_float<0>(c), unorm_to_float<1>(c), unorm_to_float<2>(c));
 }
+__device__ __forceinline__ V3 texel_at(const float4* im, size_t k) { return v3(__ldg(im + k)); }
+
+// floor(x) and (int)x of an integer-valued x, for |x| < 2^22, on the FMA and
+// integer pipes (adding 1.5 x 2^23 rounds x to an integer in the low mantissa
+// bits): the same values as floorf and the float-to-int conversion.
+__device__ __forceinline__ float floor_small(float x)
+{
+    const float r = (x + 12582912.0f) - 12582912.0f;  // x rounded to the nearest integer
+    return r > x ? r - 1.0f : r;
+}
+__device__ __forceinline__ int int_of_small(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
 
 template <class T>
-__device__ __forceinline__ V3 bilinear(const T* im, uint32_t w, uint32_t h, float s, float t, Unorm un)
+__device__ __forceinline__ V3 texel(const T* im, uint32_t w, uint32_t h, int i, int j)
 {
-    const float u = s * (float)w - 0.5f;
-    const float v = t * (float)h - 0.5f;
-    const float fi = floorf(u), fj = floorf(v);
+    if (i < 0 || j < 0 || i >= (int)w || j >= (int)h) return splat(0.0f);  // border: black
+    return texel_at(im, (size_t)j * w + i);
+}
+
+// fw, fh: the image size as floats (exact below 2^24)
+template <class T>
+__device__ __forceinline__ V3 bilinear(const T* im, uint32_t w, uint32_t h, float fw, float fh, float s, float t)
+{
+    const float u = s * fw - 0.5f;
+    const float v = t * fh - 0.5f;
+    const float fi = floor_small(u), fj = floor_small(v);
     const float al = u - fi, be = v - fj;
-    const int i0 = (int)fi, j0 = (int)fj;
+    const int i0 = int_of_small(fi), j0 = int_of_small(fj);
     const float w00 = (1.0f - al) * (1.0f - be);
     const float w10 = al * (1.0f - be);
     const float w01 = (1.0f - al) * be;
     const float w11 = al * be;
-    const V3 a = texel(im, w, h, i0, j0, un), b = texel(im, w, h, i0 + 1, j0, un);
-    const V3 c = texel(im, w, h, i0, j0 + 1, un), d = texel(im, w, h, i0 + 1, j0 + 1, un);
+    V3 a, b, c, d;
+    if (i0 >= 0 && j0 >= 0 && i0 + 1 < (int)w && j0 + 1 < (int)h) {  // all four inside
+        const size_t k = (size_t)j0 * w + i0;
+        a = texel_at(im, k);
+        b = texel_at(im, k + 1);
+        c = texel_at(im, k + w);
+        d = texel_at(im, k + w + 1);
+    } else {
+        a = texel(im, w, h, i0, j0);
+        b = texel(im, w, h, i0 + 1, j0);
+        c = texel(im, w, h, i0, j0 + 1);
+        d = texel(im, w, h, i0 + 1, j0 + 1);
+    }
     return ((a * w00 + b * w10) + c * w01) + d * w11;
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) k_present(PresentArgs p, const T* __restrict__ img0, const T* __restrict__ img1)
 {
-    __shared__ float lut[256];
-    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = (float)i / 255.0f;
-    __syncthreads();
-    const Unorm un{lut};
     const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31);
     const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= p.width || y >= p.height) return;
     const float s = ((float)x + 0.5f) / (float)p.width;
     const float t = 1.0f - ((float)y + 0.5f) / (float)p.height;
     const float inv = 1.0f / 2048.0f;  // Fullscreen.frag:12, half a texel of the reference's 1024^2 image
-    const V3 c0 = bilinear(img0, p.src_w, p.src_h, s, t, un);
-    const V3 c1 = bilinear(img1, p.src_w, p.src_h, s, t, un);
+    const float fw = (float)p.src_w, fh = (float)p.src_h;
+    const V3 c0 = bilinear(img0, p.src_w, p.src_h, fw, fh, s, t);
+    const V3 c1 = bilinear(img1, p.src_w, p.src_h, fw, fh, s, t);
     const V3 d = c0 - c1;
     const float vT = dot(d, d);
     V3 f = c0;
     if (vT > 0.0005f) {  // the four taps are only read where the variance test fires
-        const V3 n = bilinear(img0, p.src_w, p.src_h, s + 0.0f * inv, t + 1.0f * inv, un);
-        const V3 so = bilinear(img0, p.src_w, p.src_h, s + 0.0f * inv, t + -1.0f * inv, un);
-        const V3 e = bilinear(img0, p.src_w, p.src_h, s + 1.0f * inv, t + 0.0f * inv, un);
-        const V3 w = bilinear(img0, p.src_w, p.src_h, s + -1.0f * inv, t + 0.0f * inv, un);
+        const V3 n = bilinear(img0, p.src_w, p.src_h, fw, fh, s + 0.0f * inv, t + 1.0f * inv);
+        const V3 so = bilinear(img0, p.src_w, p.src_h, fw, fh, s + 0.0f * inv, t + -1.0f * inv);
+        const V3 e = bilinear(img0, p.src_w, p.src_h, fw, fh, s + 1.0f * inv, t + 0.0f * inv);
+        const V3 w = bilinear(img0, p.src_w, p.src_h, fw, fh, s + -1.0f * inv, t + 0.0f * inv);
         f = (((n + so) + e) + w) / 4.0f;
     }
     const size_t o = (size_t)y * p.width + x;
