@@ -53,6 +53,18 @@ WideNode empty_node()
 
 }  // namespace
 
+bool encode_refs(const tracer_bvh_node* nodes, uint32_t num_nodes, std::vector<tracer_bvh_node>& out)
+{
+    out.assign(nodes, nodes + num_nodes);
+    for (uint32_t i = 0; i < num_nodes; ++i) {
+        int32_t ref = nodes[i].left_or_first;
+        if (nodes[i].count > 0 && !leaf_code(nodes[i], ref)) return false;
+        out[i].left_or_first = ref;
+        out[i].count = 0;
+    }
+    return true;
+}
+
 bool collapse_wide4(const tracer_bvh_node* nodes, uint32_t num_nodes, std::vector<WideNode>& out,
                     uint32_t* depth_out)
 {

@@ -36,4 +36,12 @@ static_assert(sizeof(WideNode) == 128, "wide node is 8 x 16 bytes");
 bool collapse_wide4(const tracer_bvh_node* nodes, uint32_t num_nodes, std::vector<WideNode>& out,
                     uint32_t* depth_out);
 
+// The binary BVH as the wavefront traverses it: the same records with
+// left_or_first replaced by the record's child reference (interior: index of
+// its children pair; leaf: -1 - ((first << 6) | (count - 1))) and count = 0,
+// so the traversal reads a reference instead of decoding one.  Returns false
+// if a leaf is outside the code's range (more than 64 primitives, or first
+// beyond 2^25).
+bool encode_refs(const tracer_bvh_node* nodes, uint32_t num_nodes, std::vector<tracer_bvh_node>& out);
+
 }  // namespace vkt

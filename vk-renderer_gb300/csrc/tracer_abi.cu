@@ -45,6 +45,7 @@ template <class T> struct DevBuf {
 struct SceneBuffers {
     DevBuf<float4> tri, mats, sph_geo, sph_rec, planes, tri_nodes, sph_nodes;
     DevBuf<float4> tri_wide, sph_wide;  // the BVHs as 4-wide nodes
+    DevBuf<float4> tri_enc, sph_enc;    // the binary BVHs with pre-encoded child references
     DevBuf<uint32_t> sph_id, emit;
     uint32_t nt = 0, nm = 0, ns = 0, np = 0, ne = 0;
     uint32_t n_tri_nodes = 0, n_sph_nodes = 0;
@@ -57,6 +58,8 @@ struct SceneBuffers {
     {
         tri_wide.release();
         sph_wide.release();
+        tri_enc.release();
+        sph_enc.release();
         tri.release();
         mats.release();
         sph_geo.release();
@@ -553,6 +556,10 @@ int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
     const bool wide_ok = collapse_wide4(tnodes.data(), (uint32_t)tnodes.size(), twide, &twd) &&
                          collapse_wide4(snodes.data(), (uint32_t)snodes.size(), swide, &swd);
     s.wide_depth = twd > swd ? twd : swd;
+    std::vector<tracer_bvh_node> tenc, senc;
+    if (!encode_refs(tnodes.data(), (uint32_t)tnodes.size(), tenc) ||
+        !encode_refs(snodes.data(), (uint32_t)snodes.size(), senc))
+        return fail(c, TRACER_ERR_BAD_BVH, "a BVH leaf holds more than 64 primitives or starts beyond 2^25");
 
     cudaError_t e = upload(s.tri, tri.data(), tri.size());
     if (e == cudaSuccess) e = upload(s.mats, reinterpret_cast<const float4*>(d->materials), 3 * (size_t)s.nm);
@@ -565,6 +572,8 @@ int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
         e = upload(s.tri_nodes, reinterpret_cast<const float4*>(tnodes.data()), 2 * tnodes.size());
     if (e == cudaSuccess)
         e = upload(s.sph_nodes, reinterpret_cast<const float4*>(snodes.data()), 2 * snodes.size());
+    if (e == cudaSuccess) e = upload(s.tri_enc, reinterpret_cast<const float4*>(tenc.data()), 2 * tenc.size());
+    if (e == cudaSuccess) e = upload(s.sph_enc, reinterpret_cast<const float4*>(senc.data()), 2 * senc.size());
     if (e == cudaSuccess && wide_ok)
         e = upload(s.tri_wide, reinterpret_cast<const float4*>(twide.data()), 8 * twide.size());
     if (e == cudaSuccess && wide_ok)
@@ -651,7 +660,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     const SceneBuffers& s = c->scene;
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     const tracer_camera& cam = f->camera;
@@ -880,7 +889,7 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
@@ -949,7 +958,7 @@ namespace {
 struct PackedScene {
     std::vector<float4> tri, geo;
     std::vector<uint32_t> sid, emit;
-    std::vector<tracer_bvh_node> tnodes, snodes;
+    std::vector<tracer_bvh_node> tnodes, snodes, tenc, senc;
     std::vector<WideNode> twide, swide;
     uint32_t depth = 0, wide_depth = 0;
     bool wide = false;
@@ -999,6 +1008,11 @@ void pack_scene(const tracer_scene_desc& d, PackedScene& out)
     out.wide = collapse_wide4(out.tnodes.data(), (uint32_t)out.tnodes.size(), out.twide, &twd) &&
                collapse_wide4(out.snodes.data(), (uint32_t)out.snodes.size(), out.swide, &swd);
     out.wide_depth = twd > swd ? twd : swd;
+    if (!encode_refs(out.tnodes.data(), (uint32_t)out.tnodes.size(), out.tenc) ||
+        !encode_refs(out.snodes.data(), (uint32_t)out.snodes.size(), out.senc)) {
+        out.status = TRACER_ERR_BAD_BVH;
+        return;
+    }
     out.tri.resize(3 * (size_t)d.num_triangles);
     for (uint32_t k = 0; k < d.num_triangles; ++k) {
         const uint32_t i = tidx[k];
@@ -1069,10 +1083,10 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
             return fail(c, packed[k].status, "scene %u: BVH build or validation failed", k);
 
     // one arena per array kind, scenes back to back
-    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes, twide, swide;
+    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes, twide, swide, tenc, senc;
     std::vector<uint32_t> sid, emit;
     struct Off {
-        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit, twide, swide;
+        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit, twide, swide, tenc, senc;
     };
     std::vector<Off> off(n);
     bool wide_all = true;
@@ -1080,7 +1094,11 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
         const tracer_scene_desc& d = descs[k];
         const PackedScene& p = packed[k];
         off[k] = Off{tri.size(), mats.size(), geo.size(), rec.size(), planes.size(), tnodes.size(), snodes.size(),
-                     sid.size(), emit.size(), twide.size(), swide.size()};
+                     sid.size(), emit.size(), twide.size(), swide.size(), tenc.size(), senc.size()};
+        const float4* te = reinterpret_cast<const float4*>(p.tenc.data());
+        tenc.insert(tenc.end(), te, te + 2 * p.tenc.size());
+        const float4* se = reinterpret_cast<const float4*>(p.senc.data());
+        senc.insert(senc.end(), se, se + 2 * p.senc.size());
         wide_all = wide_all && p.wide;
         const float4* tw = reinterpret_cast<const float4*>(p.twide.data());
         twide.insert(twide.end(), tw, tw + 8 * p.twide.size());
@@ -1112,6 +1130,8 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
     if (e == cudaSuccess) e = upload(b.sph_nodes, snodes.data(), snodes.size());
     if (e == cudaSuccess) e = upload(b.sph_id, sid.data(), sid.size());
     if (e == cudaSuccess) e = upload(b.emit, emit.data(), emit.size());
+    if (e == cudaSuccess) e = upload(b.tri_enc, tenc.data(), tenc.size());
+    if (e == cudaSuccess) e = upload(b.sph_enc, senc.data(), senc.size());
     if (e == cudaSuccess && wide_all) e = upload(b.tri_wide, twide.data(), twide.size());
     if (e == cudaSuccess && wide_all) e = upload(b.sph_wide, swide.data(), swide.size());
     if (e != cudaSuccess) {
@@ -1135,7 +1155,8 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
                                       d.num_planes, (uint32_t)p.emit.size(), (uint32_t)p.tnodes.size(),
                                       (uint32_t)p.snodes.size(),
                                       wide_all ? at(b.tri_wide, off[k].twide) : nullptr,
-                                      wide_all ? at(b.sph_wide, off[k].swide) : nullptr};
+                                      wide_all ? at(b.sph_wide, off[k].swide) : nullptr,
+                                      at(b.tri_enc, off[k].tenc), at(b.sph_enc, off[k].senc)};
         b.wide_depth = std::max(b.wide_depth, p.wide_depth);
         c->batch_depth[k] = p.depth;
         c->batch_nodes[k] = (uint32_t)std::max(p.tnodes.size(), p.snodes.size());
@@ -1460,7 +1481,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};

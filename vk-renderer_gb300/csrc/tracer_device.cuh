@@ -198,6 +198,8 @@ struct DevScene {
     uint32_t n_tri_nodes, n_sph_nodes;
     const float4* tri_wide;  // 4-wide nodes (8 float4 each) of the same BVHs, or NULL
     const float4* sph_wide;
+    const float4* tri_enc;   // the binary nodes with each record's child reference pre-encoded in
+    const float4* sph_enc;   // bmin's w lane (interior: children-pair index; leaf: leaf code)
 };
 
 struct Counters {

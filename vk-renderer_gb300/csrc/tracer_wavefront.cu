@@ -40,20 +40,14 @@
 
 namespace vkt {
 
-__device__ __forceinline__ int leaf_enc(int first, int count) { return -1 - ((first << 6) | (count - 1)); }
+// The traversal reads the binary BVH with each record's child reference
+// encoded at upload (bmin.w): interior -> index of its children pair (>= 1),
+// leaf -> -1 - ((first << 6) | (count - 1)).
 __device__ __forceinline__ void leaf_dec(int enc, int& first, int& count)
 {
     const int v = -1 - enc;
     first = v >> 6;
     count = (v & 63) + 1;
-}
-// Reference to a child record: leaf -> negative code, interior -> index of its
-// children pair (>= 1).
-__device__ __forceinline__ int child_enc(float4 lo, float4 hi)
-{
-    const int cnt = __float_as_int(hi.w);
-    const int left = __float_as_int(lo.w);
-    return cnt > 0 ? leaf_enc(left, cnt) : left;
 }
 
 // The TraceArgs a path belongs to: the launch's own (single scene) or its
@@ -225,11 +219,11 @@ __device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters
         }
         return;
     }
-    L.nodes = L.pass == 0 ? sc.tri_nodes : sc.sph_nodes;
+    L.nodes = L.pass == 0 ? sc.tri_enc : sc.sph_enc;  // references pre-encoded in bmin.w
     const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
     if (STATS) cnt.c[C_NODES]++;
     float tn;
-    L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? child_enc(lo, hi) : 0;
+    L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? __float_as_int(lo.w) : 0;
     if (L.cur < 0) {  // the root is a leaf
         L.leaf = L.cur;
         L.cur = 0;
@@ -326,7 +320,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     float t0, t1;
                     const bool h0 = box_hit(L.br, lo0, hi0, L.h.t, t0);
                     const bool h1 = box_hit(L.br, lo1, hi1, L.h.t, t1);
-                    const int e0 = child_enc(lo0, hi0), e1 = child_enc(lo1, hi1);
+                    const int e0 = __float_as_int(lo0.w), e1 = __float_as_int(lo1.w);
                     if (!h0 && !h1) {
                         L.cur = pop(L, stk);
                     } else {
