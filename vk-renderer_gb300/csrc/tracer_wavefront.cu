@@ -132,25 +132,32 @@ __device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, 
     }
 }
 
-__device__ __forceinline__ int pop(Lane& L, const Stack& stk)
+// The traversal stack in shared memory: one 8-byte entry (child reference,
+// entry distance) per level, lanes interleaved (entry k of thread t at
+// k * stride + t), so a push or a pop is one access.
+struct PairStack {
+    int2* e;
+    int stride, cap;
+};
+
+__device__ __forceinline__ int pop(Lane& L, const PairStack& stk)
 {
+    const float limit = L.h.t * BOX_SLACK;
     while (L.sp > 0) {
         --L.sp;
-        const int e = stk.ci[L.sp * stk.stride];
-        const float et = stk.tn[L.sp * stk.stride];
-        if (et <= L.h.t * BOX_SLACK) return e;
+        const int2 v = stk.e[L.sp * stk.stride];
+        if (__int_as_float(v.y) <= limit) return v.x;
     }
     return 0;
 }
 
-__device__ __forceinline__ void push(Lane& L, const Stack& stk, int e, float tn, int* status)
+__device__ __forceinline__ void push(Lane& L, const PairStack& stk, int e, float tn, int* status)
 {
     if (L.sp >= stk.cap) {
         atomicCAS(status, ST_OK, ST_STACK_OVERFLOW);
         return;
     }
-    stk.ci[L.sp * stk.stride] = e;
-    stk.tn[L.sp * stk.stride] = tn;
+    stk.e[L.sp * stk.stride] = make_int2(e, __float_as_int(tn));
     ++L.sp;
 }
 
@@ -172,7 +179,7 @@ __device__ __forceinline__ void order2(float& ta, int& ra, float& tb, int& rb)
 // differs from the binary traversal only in order and in skipping interior
 // boxes, so the closest hit under strict ties is the same.
 template <bool STATS>
-__device__ __forceinline__ void visit_wide(Lane& L, int w, const Stack& stk, int* status, Counters& cnt)
+__device__ __forceinline__ void visit_wide(Lane& L, int w, const PairStack& stk, int* status, Counters& cnt)
 {
     // node = four (box min, reference) (box max, 0) records
     const float4* n = L.nodes + 8 * (size_t)w;
@@ -205,7 +212,8 @@ __device__ __forceinline__ void visit_wide(Lane& L, int w, const Stack& stk, int
 }
 
 template <bool STATS, bool WIDE>
-__device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters& cnt, const Stack& stk, int* status)
+__device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters& cnt, const PairStack& stk,
+                                           int* status)
 {
     L.prims = L.pass == 0 ? sc.tri : sc.sph_geo;
     L.leaf = 0;
@@ -238,8 +246,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     extern __shared__ int smem[];
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
-    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * BLOCK) + threadIdx.x,
-                    BLOCK, (int)a.stack_depth};
+    const PairStack stk{reinterpret_cast<int2*>(smem) + threadIdx.x, BLOCK, (int)a.stack_depth};
     const uint32_t total = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
@@ -326,15 +333,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     } else {
                         const bool swap = h1 && (!h0 || t1 < t0);
                         L.cur = swap ? e1 : e0;
-                        if (h0 && h1) {
-                            if (L.sp >= stk.cap) {
-                                atomicCAS(a.status, ST_OK, ST_STACK_OVERFLOW);
-                            } else {
-                                stk.ci[L.sp * stk.stride] = swap ? e0 : e1;
-                                stk.tn[L.sp * stk.stride] = swap ? t0 : t1;
-                                ++L.sp;
-                            }
-                        }
+                        if (h0 && h1) push(L, stk, swap ? e0 : e1, swap ? t0 : t1, a.status);
                     }
                     if (L.cur < 0 && L.leaf == 0) {
                         L.leaf = L.cur;
