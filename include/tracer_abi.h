@@ -203,6 +203,9 @@ typedef struct tracer_trace_params {
     uint32_t bvh_width;     /* wavefront traversal: 0 = auto (= 2), 2 = the binary BVH, 4 = 4-wide nodes
                                collapsed from it (same boxes, same hits; measured slower on sparse
                                triangle soups, where it tests boxes the binary traversal culls) */
+    uint32_t tail_paths;    /* wavefront: once fewer than this many paths are live, one kernel runs each of
+                               them to the end of its pixel (remaining bounces and samples) instead of
+                               further rounds; 0 = auto, 1 = never.  Same images either way. */
 } tracer_trace_params;
 
 typedef struct tracer_stats {
@@ -301,9 +304,22 @@ typedef struct tracer_timings {
     float shade_ms;     /* wavefront: sum over rounds of the shade kernel */
     uint32_t rounds;    /* wavefront rounds (extend + shade) */
     uint32_t launches;  /* kernels launched */
+    float finish_ms;    /* wavefront: the kernel that finished the last paths (tail_paths), 0 if none ran */
 } tracer_timings;
 int tracer_set_profiling(tracer_ctx* ctx, int enable);
 int tracer_last_timings(tracer_ctx* ctx, tracer_timings* out);
+
+/* Per-round detail of the last single-scene wavefront trace made with
+ * profiling on: live paths at the start of each round and its kernel times.
+ * When the finishing kernel ran, the last entry is its own (finish = 1, its
+ * time in extend_ms).  Writes min(cap, entries) records, the count to *n. */
+typedef struct tracer_round_info {
+    uint32_t paths;   /* paths queued for the round */
+    uint32_t finish;  /* 1: the finishing kernel */
+    float extend_ms;
+    float shade_ms;
+} tracer_round_info;
+int tracer_last_rounds(tracer_ctx* ctx, tracer_round_info* out, uint32_t cap, uint32_t* n);
 
 /* Trace that allocates no memory during the call.  No counterpart in the
  * reference (its Vulkan device allocates all its buffers up front in
@@ -316,7 +332,10 @@ int tracer_last_timings(tracer_ctx* ctx, tracer_timings* out);
  * has already allocated.  Such a caller creates the context and uploads the
  * scene once at start-up, then calls this entry point per frame.
  *
- * It runs the wavefront kernels on the scene uploaded to ctx and writes the
+ * It runs the wavefront kernels on the scene uploaded to ctx (with no queue
+ * length read back: when the image has fewer pixels than tail_paths -- always
+ * with the automatic threshold -- the generate kernel and one finishing
+ * launch, else every round) and writes the
  * image straight into caller-owned device buffers: rgba8_out (w*h*4 bytes)
  * and/or rgba32f_out (w*h*16 bytes); either may be NULL, not both.  The
  * wavefront's path state, queues and counters live in one fixed array of

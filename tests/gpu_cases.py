@@ -36,11 +36,12 @@ def scene_bvhs(sc: S.Scene, tri_bvh=None, sphere_bvh=None):
 
 
 def run_gpu(tr: abi.Tracer, sc: S.Scene, fr, w, h, spp, depth, rr_start=0, sky=(0, 0, 0), tie=abi.TIES_STRICT,
-            kernel=abi.KERNEL_PLAIN, block=0, tri_bvh=None, sphere_bvh=None, stats=True):
+            kernel=abi.KERNEL_PLAIN, block=0, tri_bvh=None, sphere_bvh=None, stats=True, tail_paths=0):
     tri_bvh, sphere_bvh = scene_bvhs(sc, tri_bvh, sphere_bvh)
     tr.upload_scene(sc, tri_bvh=tri_bvh, sphere_bvh=sphere_bvh)
     p = abi.Tracer.params(w, h, spp=spp, max_depth=depth, rr_start=rr_start, sky=sky, tie_mode=tie, kernel=kernel,
-                          block=block, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F, abi.AOV_PRIMARY_HIT), stats=stats)
+                          block=block, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F, abi.AOV_PRIMARY_HIT), stats=stats,
+                          tail_paths=tail_paths)
     tr.trace(fr, p)
     out = {"rgba32f": tr.readback(abi.AOV_RGBA32F), "rgba8": tr.readback(abi.AOV_RGBA8)}
     hit = tr.readback(abi.AOV_PRIMARY_HIT)

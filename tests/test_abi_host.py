@@ -34,7 +34,7 @@ int main(void) {
   S(tracer_bvh_node); P(tracer_bvh_node, bmin); P(tracer_bvh_node, left_or_first); P(tracer_bvh_node, bmax);
   P(tracer_bvh_node, count);
   S(tracer_stats); S(tracer_trace_params); S(tracer_scene_desc); S(tracer_timings);
-  S(tracer_present_params); S(tracer_camera_controller); S(tracer_input_frame);
+  S(tracer_present_params); S(tracer_camera_controller); S(tracer_input_frame); S(tracer_round_info);
   P(tracer_camera_controller, front); P(tracer_camera_controller, light_pos); P(tracer_input_frame, cursor_x);
   return 0;
 }
@@ -97,6 +97,7 @@ def test_numpy_dtypes_match_header(layout):
     assert ctypes.sizeof(abi.PresentParams) == layout["tracer_present_params"]
     assert ctypes.sizeof(abi.CameraController) == layout["tracer_camera_controller"]
     assert ctypes.sizeof(abi.InputFrame) == layout["tracer_input_frame"]
+    assert ctypes.sizeof(abi.RoundInfo) == layout["tracer_round_info"]
     assert abi.CameraController.front.offset == layout["tracer_camera_controller.front"]
     assert abi.CameraController.light_pos.offset == layout["tracer_camera_controller.light_pos"]
     assert abi.InputFrame.cursor_x.offset == layout["tracer_input_frame.cursor_x"]

@@ -120,6 +120,10 @@ struct tracer_ctx {
     cudaEvent_t prof_begin = nullptr, prof_end = nullptr;
     uint32_t last_rounds = 0, last_launches = 0;
     uint32_t last_prof_rounds = 0;  // rounds of the last trace with per-kernel events recorded
+    DevBuf<uint32_t> round_paths;   // profiling: live paths at the start of each round (+ the finish)
+    uint32_t last_round_entries = 0;
+    bool last_finish = false;       // the finishing kernel ran in the last trace
+    uint32_t last_handover = 0;     // rounds before the finishing kernel in the last trace (0: none ran)
     int last_kernel = 0;
     // batch of scenes (tracer_upload_scenes / tracer_trace_batched)
     SceneBuffers batch;                 // arena: every scene's arrays back to back
@@ -138,6 +142,8 @@ struct tracer_ctx {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<uint64_t> graph_key;
+    uint64_t graph_rounds = 0;  // rounds in the graph, then the finishing kernel if graph_finish
+    bool graph_finish = false;
     AdjBuffers adj;  // adjoint: dL/dI, linear image and gradient buffers
     // present pass and draw loop
     uint64_t scene_version = 0;       // bumped by every scene or material upload
@@ -267,10 +273,16 @@ cudaEvent_t prof_event(tracer_ctx* c, size_t i)
 // Launches the wavefront: generate, then rounds of extend + shade until the
 // path queue is empty (read back a few rounds behind the launches) or
 // max_rounds is reached (no path needs more than spp * max_depth rounds).
+// Once a read-back count is below tail, the finishing kernel runs the paths
+// still queued to the end of their pixels and the rounds stop (counts never
+// grow from round to round, so the lagged count bounds the current one).
+// tail: 0 = the extend kernel's resident threads (below one path per lane, a
+// round costs about the latency of its slowest ray, whatever its size),
+// 1 = never.
 // With adj, the adjoint's generate and shade stages run instead of the
-// forward ones (the extend stage is shared).
+// forward's (a.linear = the forward image), and there is no finishing kernel.
 int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots, uint64_t max_rounds,
-                  uint32_t stack, uint32_t wavefront, cudaStream_t st, const AdjWf* adj = nullptr)
+                  uint32_t stack, uint32_t wavefront, uint32_t tail, cudaStream_t st, const AdjWf* adj = nullptr)
 {
     WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
                c->wf_prim0.p, {c->wf_q0.p, c->wf_q1.p}, c->wf_count.p, c->wf_scene.p};
@@ -280,7 +292,17 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     wc.extend_grid = (uint32_t)(per * c->sm_count);
     const size_t sg = (nslots + 255) / 256;
     wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
+    if (tail == 0) tail = wc.extend_grid * wc.block;
+    const int fin_per = (adj || tail <= 1) ? 0 : wf_finish_blocks_per_sm(wc, stack);
+    if (fin_per <= 0) tail = 0;
     cudaError_t e = cudaSuccess;
+    if (c->profiling) {
+        e = dalloc(c->round_paths, (size_t)max_rounds + 1);
+        if (e != cudaSuccess) return cuda_fail(c, e, "round statistics");
+    }
+    c->last_round_entries = 0;
+    c->last_finish = false;
+    c->last_handover = 0;
     if (adj) {
         e = cudaMemsetAsync(c->wf_count.p, 0, 3 * sizeof(uint32_t), st);
         if (e == cudaSuccess) e = wf_launch_adj_generate(a, ws, *adj, st);
@@ -290,7 +312,11 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     c->last_launches += 1;
     for (uint64_t r = 0; r < max_rounds && e == cudaSuccess; ++r) {
         const int qsel = (int)(r & 1);
-        if (c->profiling) cudaEventRecord(prof_event(c, 3 * r), st);
+        if (c->profiling) {
+            cudaMemcpyAsync(c->round_paths.p + r, c->wf_count.p + qsel, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+            c->last_round_entries = (uint32_t)(r + 1);
+            cudaEventRecord(prof_event(c, 3 * r), st);
+        }
         e = wf_launch_extend(a, ws, wc, qsel, st);
         if (c->profiling) cudaEventRecord(prof_event(c, 3 * r + 1), st);
         if (e == cudaSuccess) e = adj ? wf_launch_adj_shade(a, ws, *adj, wc, qsel, st) : wf_launch_shade(a, ws, wc, qsel, st);
@@ -307,7 +333,27 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
             const int old = (int)((r - kCountLag) % kCountSlots);
             int w = wait_event(c, c->count_events[old]);
             if (w != TRACER_OK) return w;
-            if (c->pinned_counts[old] == 0) break;
+            const uint32_t live = c->pinned_counts[old];
+            if (live == 0) break;
+            if (live < tail && r + 1 < max_rounds) {
+                const uint64_t f = r + 1;
+                const int fq = (int)(f & 1);
+                const uint64_t blocks = ((uint64_t)live + 127) / 128;
+                const uint64_t cap = (uint64_t)fin_per * c->sm_count;
+                wc.finish_grid = (uint32_t)(blocks < cap ? blocks : cap);
+                if (c->profiling) {
+                    cudaMemcpyAsync(c->round_paths.p + f, c->wf_count.p + fq, sizeof(uint32_t),
+                                    cudaMemcpyDeviceToDevice, st);
+                    c->last_round_entries = (uint32_t)(f + 1);
+                    cudaEventRecord(prof_event(c, 3 * f), st);
+                }
+                e = wf_launch_finish(a, ws, wc, fq, st);
+                if (c->profiling) cudaEventRecord(prof_event(c, 3 * f + 1), st);
+                c->last_launches += 1;
+                c->last_finish = true;
+                c->last_handover = (uint32_t)f;
+                break;
+            }
         }
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
@@ -693,6 +739,8 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     c->last_kernel = kernel;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
+    c->last_round_entries = 0;
+    c->last_finish = false;
     c->last_launches = 0;
     if (c->profiling) cudaEventRecord(c->prof_begin, st);
 
@@ -716,7 +764,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         r = pick_width(c, p, wstack, wc.wide);
         if (r != TRACER_OK) return r;
         a.stack_depth = wstack;
-        r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, st);
+        r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, p->tail_paths, st);
         if (r != TRACER_OK) return r;
     }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
@@ -751,6 +799,43 @@ int tracer_last_timings(tracer_ctx* c, tracer_timings* out)
             if (cudaEventElapsedTime(&ms, c->prof_events[3 * i + 1], c->prof_events[3 * i + 2]) == cudaSuccess)
                 out->shade_ms += ms;
         }
+        const size_t f = c->last_prof_rounds;
+        if (c->last_finish && 3 * f + 1 < c->prof_events.size() &&
+            cudaEventElapsedTime(&ms, c->prof_events[3 * f], c->prof_events[3 * f + 1]) == cudaSuccess)
+            out->finish_ms = ms;
+    }
+    return TRACER_OK;
+}
+
+int tracer_last_rounds(tracer_ctx* c, tracer_round_info* out, uint32_t cap, uint32_t* n)
+{
+    if (!c || !n || (cap && !out)) return TRACER_ERR_INVALID_ARG;
+    *n = 0;
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    if (!c->profiling) return fail(c, TRACER_ERR_INVALID_ARG, "profiling is off (tracer_set_profiling)");
+    if (c->last_kernel != TRACER_KERNEL_WAVEFRONT || c->last_round_entries == 0) return TRACER_OK;
+    const uint32_t rounds = c->last_prof_rounds;
+    const uint32_t entries = c->last_round_entries < rounds + (c->last_finish ? 1u : 0u)
+                                 ? c->last_round_entries
+                                 : rounds + (c->last_finish ? 1u : 0u);
+    std::vector<uint32_t> paths(entries);
+    cudaError_t e = cudaMemcpy(paths.data(), c->round_paths.p, sizeof(uint32_t) * entries, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "reading round statistics");
+    *n = entries;
+    for (uint32_t i = 0; i < entries && i < cap; ++i) {
+        tracer_round_info& o = out[i];
+        o.paths = paths[i];
+        o.finish = (c->last_finish && i == rounds) ? 1u : 0u;
+        o.extend_ms = 0.0f;
+        o.shade_ms = 0.0f;
+        float ms = 0.0f;
+        if (3 * (size_t)i + 1 < c->prof_events.size() &&
+            cudaEventElapsedTime(&ms, c->prof_events[3 * i], c->prof_events[3 * i + 1]) == cudaSuccess)
+            o.extend_ms = ms;
+        if (!o.finish && 3 * (size_t)i + 2 < c->prof_events.size() &&
+            cudaEventElapsedTime(&ms, c->prof_events[3 * i + 1], c->prof_events[3 * i + 2]) == cudaSuccess)
+            o.shade_ms = ms;
     }
     return TRACER_OK;
 }
@@ -939,12 +1024,23 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     // counters; statistics are not collected here.
     cudaError_t e = cudaMemsetAsync(a.status, 0, sizeof(int), st);
     if (e == cudaSuccess) e = wf_launch_generate(a, ws, wc, st);
-    // Every round is launched (no queue length is read back to the host); a
-    // round with an empty queue returns at once.
-    const uint32_t rounds = p->spp * p->max_depth + 1;
-    for (uint32_t k = 0; k < rounds && e == cudaSuccess; ++k) {
-        e = wf_launch_extend(a, ws, wc, (int)(k & 1), st);
-        if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, (int)(k & 1), st);
+    // No queue length is read back to the host.  Below the hand-over
+    // threshold from the start (always, with the automatic threshold: the
+    // image is smaller than the extend kernel's resident threads), the
+    // finishing kernel traces every pixel in one launch; otherwise every round
+    // is launched, and a round with an empty queue returns at once.
+    const uint32_t tail = p->tail_paths ? p->tail_paths : wc.extend_grid * wc.block;
+    const int fin_per = tail > npx ? wf_finish_blocks_per_sm(wc, stack) : 0;
+    if (fin_per > 0) {
+        const size_t blocks = (npx + 127) / 128, cap = (size_t)fin_per * c->sm_count;
+        wc.finish_grid = (uint32_t)(blocks < cap ? blocks : cap);
+        if (e == cudaSuccess) e = wf_launch_finish(a, ws, wc, 0, st);
+    } else {
+        const uint32_t rounds = p->spp * p->max_depth + 1;
+        for (uint32_t k = 0; k < rounds && e == cudaSuccess; ++k) {
+            e = wf_launch_extend(a, ws, wc, (int)(k & 1), st);
+            if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, (int)(k & 1), st);
+        }
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "no-alloc trace launch");
     return TRACER_OK;
@@ -1284,6 +1380,8 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
     c->last_kernel = kernel;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
+    c->last_round_entries = 0;
+    c->last_finish = false;
     c->last_launches = 0;
     if (c->profiling) cudaEventRecord(c->prof_begin, st);
 
@@ -1310,7 +1408,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         wc.slots = c->batch_slots.p;
         wc.nslots = n;
         if (!use_graph) {
-            r = run_wavefront(c, a, wc, total, max_rounds, stack, p0.wavefront, st);
+            r = run_wavefront(c, a, wc, total, max_rounds, stack, p0.wavefront, p0.tail_paths, st);
             if (r != TRACER_OK) return r;
         } else {
             WfState ws{c->wf_ray_o.p, c->wf_ray_d.p, c->wf_hit.p, c->wf_acc.p, c->wf_mask.p, c->wf_accum.p,
@@ -1323,7 +1421,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
             wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
             // the graph bakes in sizes, launch shapes and buffer addresses
             std::vector<uint64_t> key = {n, total, max_rounds, block, stack, (uint64_t)stats, wc.extend_grid,
-                                         (uint64_t)wide,
+                                         (uint64_t)wide, p0.tail_paths,
                                          (uint64_t)(uintptr_t)c->wf_ray_o.p, (uint64_t)(uintptr_t)c->batch_slots.p,
                                          (uint64_t)(uintptr_t)c->b_rgba8.p, (uint64_t)(uintptr_t)c->b_rgba32f.p,
                                          (uint64_t)(uintptr_t)c->b_hit.p, mask};
@@ -1333,14 +1431,29 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
                 c->graph_exec = nullptr;
                 c->graph = nullptr;
                 c->graph_key.clear();
+                // The graph has no queue lengths to look at, so the round at
+                // which the finishing kernel takes over is the one a traced
+                // run of this batch reaches (launched here, with read-backs).
+                // Any frame is still traced completely: the finishing kernel
+                // runs whatever paths are queued after that round.
+                r = run_wavefront(c, a, wc, total, max_rounds, stack, p0.wavefront, p0.tail_paths, st);
+                if (r != TRACER_OK) return r;
+                const uint64_t rounds = c->last_handover ? c->last_handover : max_rounds;
+                const int fin_per = c->last_handover ? wf_finish_blocks_per_sm(wc, stack) : 0;
+                c->graph_rounds = rounds;
+                c->graph_finish = fin_per > 0;
                 cudaStream_t cap;
                 e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
                 if (e != cudaSuccess) return cuda_fail(c, e, "graph capture stream");
                 e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) e = wf_launch_generate(a, ws, wc, cap);
-                for (uint64_t k = 0; k < max_rounds && e == cudaSuccess; ++k) {
+                for (uint64_t k = 0; k < rounds && e == cudaSuccess; ++k) {
                     e = wf_launch_extend(a, ws, wc, (int)(k & 1), cap);
                     if (e == cudaSuccess) e = wf_launch_shade(a, ws, wc, (int)(k & 1), cap);
+                }
+                if (e == cudaSuccess && fin_per > 0) {
+                    wc.finish_grid = (uint32_t)(fin_per * c->sm_count);
+                    e = wf_launch_finish(a, ws, wc, (int)(rounds & 1), cap);
                 }
                 cudaGraph_t g = nullptr;
                 cudaError_t e2 = cudaStreamEndCapture(cap, &g);
@@ -1355,8 +1468,11 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
                 c->graph_key = key;
             }
             e = cudaGraphLaunch(c->graph_exec, st);
-            c->last_rounds = (uint32_t)max_rounds;
-            c->last_launches = (uint32_t)(1 + 2 * max_rounds);
+            c->last_rounds = (uint32_t)c->graph_rounds;
+            c->last_launches = (uint32_t)(1 + 2 * c->graph_rounds + (c->graph_finish ? 1 : 0));
+            c->last_finish = c->graph_finish;
+            c->last_prof_rounds = 0;  // the graph's rounds are not timed one by one
+            c->last_round_entries = 0;
         }
     }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
@@ -1502,6 +1618,8 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     a.status = c->status.p;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
+    c->last_round_entries = 0;
+    c->last_finish = false;
     c->last_mask = 1u << TRACER_AOV_STATS;
     c->width = p->width;
     c->height = p->height;
@@ -1526,7 +1644,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         c->last_launches = 1;  // + generate, rounds; the FP64-to-float conversion
         if (c->profiling) cudaEventRecord(c->prof_begin, st);
         // a sample takes at most max_depth rounds in each pass
-        r = run_wavefront(c, a, wc, npx, 2 * (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, st, &aw);
+        r = run_wavefront(c, a, wc, npx, 2 * (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, 1, st, &aw);
         if (r != TRACER_OK) return r;
     } else {
         c->last_kernel = 3;
@@ -1664,6 +1782,8 @@ extern "C" int tracer_present(tracer_ctx* c, const void* image0, const void* ima
     c->last_kernel = 0;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
+    c->last_round_entries = 0;
+    c->last_finish = false;
     return present_into(c, pp, src[0], src[1], src_width, src_height, src_aov == TRACER_AOV_RGBA32F, out, st, true);
 }
 
@@ -1796,6 +1916,8 @@ extern "C" int tracer_trace_whitted(tracer_ctx* c, const tracer_frame* f, const 
     c->last_kernel = 0;
     c->last_rounds = 0;
     c->last_prof_rounds = 0;
+    c->last_round_entries = 0;
+    c->last_finish = false;
     c->last_launches = 1;
     if (c->profiling) cudaEventRecord(c->prof_begin, st);
     e = launch_whitted(a, stats, st);

@@ -21,6 +21,9 @@
 //                continues where the last one stopped (the shader's rand_salt
 //                runs across samples, :578-581); a finished pixel is resolved
 //                (:585-592).
+//   wf_finish    for the last rounds, when few paths are live: each thread
+//                runs queued paths to the end of their pixels (all remaining
+//                bounces and samples), without per-round launches.
 //
 // MULTI = true runs many scenes of different size and resolution in the same
 // queues (the batched form): every path slot belongs to one scene, whose
@@ -437,6 +440,77 @@ __global__ void __launch_bounds__(128) wf_extend_linear(TraceArgs a, WfState s, 
     if (STATS) flush_counters(a, cnt);
 }
 
+// ------------------------------------------------------------- path state --
+// One path slot between rounds, unpacked from the WfState arrays.
+struct PathRegs {
+    Ray ray;
+    V3 acc, mask, accum;
+    float t0;  // t of the pixel's primary hit (-1: none)
+    uint32_t prim0, sample, depth;
+    Rng g;
+};
+
+__device__ __forceinline__ void load_path(const WfState& s, const TraceArgs& A, uint32_t pid, uint32_t x, uint32_t y,
+                                          PathRegs& p)
+{
+    const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
+    const float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
+    p.ray = Ray{v3(ro), v3(rd)};
+    p.acc = v3(acc4);
+    p.mask = v3(mask4);
+    p.accum = v3(accum4);
+    p.t0 = mask4.w;
+    p.prim0 = s.prim0[pid];
+    const uint32_t sd = __float_as_uint(accum4.w);
+    p.sample = sd >> 16;
+    p.depth = sd & 0xFFFFu;
+    p.g.salt = acc4.w;
+    p.g.cx = (float)x / (float)A.width;
+    p.g.cy = (float)y / (float)A.height;
+}
+
+__device__ __forceinline__ void store_path(const WfState& s, uint32_t pid, const PathRegs& p)
+{
+    s.ray_o[pid] = make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, depth_tmax(p.depth));
+    s.ray_d[pid] = make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, 0.0f);
+    s.acc[pid] = make_float4(p.acc.x, p.acc.y, p.acc.z, p.g.salt);
+    s.mask[pid] = make_float4(p.mask.x, p.mask.y, p.mask.z, p.t0);
+    s.accum[pid] = make_float4(p.accum.x, p.accum.y, p.accum.z, __uint_as_float((p.sample << 16) | p.depth));
+    s.prim0[pid] = p.prim0;
+}
+
+// The rest of one depth iteration after its closest hit h (Tracer.comp:441-549:
+// clamp, sky, scatter, next-event estimation, Russian roulette), then the
+// sample and pixel bookkeeping (:578-592): the next depth, else the pixel's
+// next sample (its RNG continues where the last sample stopped), else the
+// resolve.  Returns true while the pixel has another ray to trace: p.ray, with
+// tmax depth_tmax(p.depth).
+template <class TR>
+__device__ __forceinline__ bool advance_path(TR& tr, const TraceArgs& A, uint32_t x, uint32_t y, const Hit& h,
+                                             PathRegs& p)
+{
+    const bool found = h.kind != 0;
+    if (p.sample == 0 && p.depth == 0) {
+        p.prim0 = found ? h.prim : NO_PRIM;
+        p.t0 = found ? h.t : -1.0f;
+    }
+    p.acc = vclamp01(p.acc);
+    const bool cont = shade_bounce(tr, A, p.depth, found, h, p.ray, p.acc, p.mask, p.g);
+    p.depth++;
+    if (cont && p.depth < A.max_depth) return true;
+    p.accum = p.accum + p.acc;
+    p.sample++;
+    p.depth = 0;
+    if (p.sample < A.spp) {
+        p.ray = primary_ray(A, x, y);
+        p.acc = splat(0.0f);
+        p.mask = splat(1.0f);
+        return true;
+    }
+    resolve_pixel(A, x, y, p.accum, p.g, p.prim0, p.t0);
+    return false;
+}
+
 // ------------------------------------------------------------------- shade --
 template <int TIE, bool BVH, bool STATS, bool MULTI>
 __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
@@ -445,7 +519,7 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
     const uint32_t n = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     uint32_t* next = qsel ? s.queue[0] : s.queue[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // extend's fetch cursor for the next round
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // fetch cursor of the next round
     Counters cnt;
 #pragma unroll
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
@@ -454,67 +528,69 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t qi = base + threadIdx.x;
-        const bool active = qi < n;
         bool again = false;
         uint32_t pid = 0;
-        if (active) {
+        if (qi < n) {
             pid = queue[qi];
             const TraceArgs& A = SCENE_ARGS(MULTI, a, slots, MULTI ? s.scene_of[pid] : 0);
             Tracer<TIE, BVH, STATS> tr{A.sc, stk, cnt, a.status, A.trav_limit};
             const uint32_t p = pid - A.pixel_base;
             const uint32_t x = p % A.width, y = p / A.width;
-            const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
+            PathRegs ps;
+            load_path(s, A, pid, x, y, ps);
             const uint4 hr = s.hit[pid];
-            const float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
-            uint32_t prim0 = s.prim0[pid];
-            const uint32_t sd = __float_as_uint(accum4.w);
-            uint32_t sample = sd >> 16, depth = sd & 0xFFFFu;
-            Rng g;
-            g.salt = acc4.w;
-            g.cx = (float)x / (float)A.width;
-            g.cy = (float)y / (float)A.height;
-            V3 acc = vclamp01(v3(acc4));
-            V3 mask = v3(mask4);
             Hit h;
             h.t = __uint_as_float(hr.x);
             h.prim = hr.y;
             h.slot = hr.z;
             h.kind = (int)hr.w;
-            const bool found = h.kind != 0;
-            float t0 = mask4.w;
-            if (sample == 0 && depth == 0) {
-                prim0 = found ? h.prim : NO_PRIM;
-                t0 = found ? h.t : -1.0f;
-            }
-            Ray ray{v3(ro), v3(rd)};
-            const bool cont = shade_bounce(tr, A, depth, found, h, ray, acc, mask, g);
-            depth++;
-            V3 accum = v3(accum4);
-            if (cont && depth < A.max_depth) {
-                again = true;
-            } else {
-                accum = accum + acc;
-                sample++;
-                depth = 0;
-                if (sample < A.spp) {
-                    ray = primary_ray(A, x, y);
-                    acc = splat(0.0f);
-                    mask = splat(1.0f);
-                    again = true;
-                } else {
-                    resolve_pixel(A, x, y, accum, g, prim0, t0);
-                }
-            }
-            if (again) {
-                s.ray_o[pid] = make_float4(ray.o.x, ray.o.y, ray.o.z, depth_tmax(depth));
-                s.ray_d[pid] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
-                s.acc[pid] = make_float4(acc.x, acc.y, acc.z, g.salt);
-                s.mask[pid] = make_float4(mask.x, mask.y, mask.z, t0);
-                s.accum[pid] = make_float4(accum.x, accum.y, accum.z, __uint_as_float((sample << 16) | depth));
-                s.prim0[pid] = prim0;
-            }
+            again = advance_path(tr, A, x, y, h, ps);
+            if (again) store_path(s, pid, ps);
         }
         warp_append(again, pid, next, &s.count[qsel ^ 1]);
+    }
+    if (STATS) flush_counters(a, cnt);
+}
+
+// ------------------------------------------------------------------ finish --
+// Runs every queued path to the end of its pixel in one launch: a thread takes
+// a path and traces and shades it bounce after bounce, sample after sample,
+// with the per-thread traversal, until the pixel is resolved; then it takes
+// the next.  For the last rounds of a wavefront, when few paths are live:
+// they then need no launches per round and do not wait each round for that
+// round's slowest ray.  The operations per pixel are those of extend + shade,
+// in the same order, so the results are identical.
+// First path of a thread: queue entry = its global index; later ones from the
+// cursor count[2] (zeroed by the shade that wrote the queue), offset by the
+// number of threads.
+template <int TIE, bool BVH, bool STATS, bool MULTI>
+__global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
+{
+    extern __shared__ int smem[];
+    const uint32_t n = s.count[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
+                    (int)blockDim.x, (int)a.stack_depth};
+    const uint32_t threads = gridDim.x * blockDim.x;
+    uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    while (qi < n) {
+        const uint32_t pid = queue[qi];
+        const TraceArgs& A = SCENE_ARGS(MULTI, a, slots, MULTI ? s.scene_of[pid] : 0);
+        Tracer<TIE, BVH, STATS> tr{A.sc, stk, cnt, a.status, A.trav_limit};
+        const uint32_t p = pid - A.pixel_base;
+        const uint32_t x = p % A.width, y = p / A.width;
+        PathRegs ps;
+        load_path(s, A, pid, x, y, ps);
+        for (;;) {
+            Hit h;
+            h.t = depth_tmax(ps.depth);
+            tr.trace(ps.ray, h, false);
+            if (!advance_path(tr, A, x, y, h, ps)) break;
+        }
+        qi = n > threads ? threads + atomicAdd(&s.count[2], 1u) : n;
     }
     if (STATS) flush_counters(a, cnt);
 }
@@ -558,6 +634,25 @@ static cudaError_t shade_t(const TraceArgs& a, const WfState& s, const WfConfig&
     return cudaGetLastError();
 }
 
+template <int TIE, bool BVH, bool STATS, bool MULTI>
+static cudaError_t finish_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    auto k = wf_finish<TIE, BVH, STATS, MULTI>;
+    const size_t smem = BVH ? (size_t)a.stack_depth * 128 * 8 : 0;
+    smem_attr(k, smem);
+    k<<<c.finish_grid, 128, smem, st>>>(a, s, qsel, c.slots);
+    return cudaGetLastError();
+}
+
+template <int TIE, bool BVH, bool STATS, bool MULTI>
+static int finish_occ(size_t smem)
+{
+    auto k = wf_finish<TIE, BVH, STATS, MULTI>;
+    smem_attr(k, smem);
+    int n = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, smem) == cudaSuccess ? n : 0;
+}
+
 // Template selection: ties, BVH (strict only), statistics, multi-scene (BVH only).
 #define WF_DISPATCH(fn)                                                                                    \
     if (c.multi) {                                                                                         \
@@ -591,6 +686,23 @@ cudaError_t wf_launch_extend(const TraceArgs& a, const WfState& s, const WfConfi
 cudaError_t wf_launch_shade(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
     WF_DISPATCH(shade_t)
+}
+
+cudaError_t wf_launch_finish(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
+{
+    WF_DISPATCH(finish_t)
+}
+
+int wf_finish_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
+{
+    const size_t smem = c.bvh ? (size_t)stack_depth * 128 * 8 : 0;
+    if (c.multi) return c.stats ? finish_occ<TIE_STRICT, true, true, true>(smem)
+                                : finish_occ<TIE_STRICT, true, false, true>(smem);
+    if (c.tie == TIE_REFERENCE) return c.stats ? finish_occ<TIE_REFERENCE, false, true, false>(smem)
+                                               : finish_occ<TIE_REFERENCE, false, false, false>(smem);
+    if (c.bvh) return c.stats ? finish_occ<TIE_STRICT, true, true, false>(smem)
+                              : finish_occ<TIE_STRICT, true, false, false>(smem);
+    return c.stats ? finish_occ<TIE_STRICT, false, true, false>(smem) : finish_occ<TIE_STRICT, false, false, false>(smem);
 }
 
 template <int TIE, bool STATS, bool MULTI, int BLOCK>

@@ -30,6 +30,7 @@ struct WfConfig {
     int wide;                 // extend traverses the 4-wide nodes (every scene has them)
     uint32_t block;           // extend kernel threads per block: 64, 128 or 256
     uint32_t extend_grid, shade_grid;
+    uint32_t finish_grid;     // blocks of 128 threads of the finishing kernel
     const TraceArgs* slots;   // batched: device table of per-scene arguments
     uint32_t nslots;
 };
@@ -37,6 +38,8 @@ struct WfConfig {
 cudaError_t wf_launch_generate(const TraceArgs& a, const WfState& s, const WfConfig& c, cudaStream_t st);
 cudaError_t wf_launch_extend(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st);
 cudaError_t wf_launch_shade(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st);
+cudaError_t wf_launch_finish(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st);
 int wf_extend_blocks_per_sm(const WfConfig& c, uint32_t stack_depth);
+int wf_finish_blocks_per_sm(const WfConfig& c, uint32_t stack_depth);
 
 }  // namespace vkt

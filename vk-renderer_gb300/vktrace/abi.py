@@ -42,6 +42,7 @@ EXPORTED_SYMBOLS = [
     "tracer_readback_scene", "tracer_trace_adjoint", "tracer_present", "tracer_draw", "tracer_draw_reset",
     "tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update", "tracer_camera_move",
     "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script", "tracer_trace_whitted",
+    "tracer_last_rounds",
 ]
 PRESENT_PINGPONG, PRESENT_ACCUMULATE = 0, 1
 KEY_W, KEY_S, KEY_A, KEY_D, KEY_R, KEY_F = 1, 2, 4, 8, 16, 32
@@ -74,7 +75,7 @@ class TraceParams(ctypes.Structure):
         ("max_depth", ctypes.c_uint32), ("rr_start", ctypes.c_uint32), ("sky", ctypes.c_float * 3),
         ("tie_mode", ctypes.c_int32), ("kernel", ctypes.c_int32), ("block", ctypes.c_uint32),
         ("stack_depth", ctypes.c_uint32), ("wavefront", ctypes.c_uint32), ("aov_mask", ctypes.c_uint32),
-        ("stats", ctypes.c_uint32), ("bvh_width", ctypes.c_uint32),
+        ("stats", ctypes.c_uint32), ("bvh_width", ctypes.c_uint32), ("tail_paths", ctypes.c_uint32),
     ]
 
 
@@ -96,7 +97,12 @@ class InputFrame(ctypes.Structure):
 
 class Timings(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_float), ("extend_ms", ctypes.c_float), ("shade_ms", ctypes.c_float),
-                ("rounds", ctypes.c_uint32), ("launches", ctypes.c_uint32)]
+                ("rounds", ctypes.c_uint32), ("launches", ctypes.c_uint32), ("finish_ms", ctypes.c_float)]
+
+
+class RoundInfo(ctypes.Structure):
+    _fields_ = [("paths", ctypes.c_uint32), ("finish", ctypes.c_uint32), ("extend_ms", ctypes.c_float),
+                ("shade_ms", ctypes.c_float)]
 
 
 _lib = None
@@ -130,6 +136,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_validate_bvh.argtypes = [i32, vp, u32, vp, u32, vp, ctypes.POINTER(u32)]
     lib.tracer_set_profiling.argtypes = [vp, i32]
     lib.tracer_last_timings.argtypes = [vp, ctypes.POINTER(Timings)]
+    lib.tracer_last_rounds.argtypes = [vp, ctypes.POINTER(RoundInfo), u32, ctypes.POINTER(u32)]
     lib.tracer_trace_noalloc.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp, vp, vp]
     lib.tracer_upload_scenes.argtypes = [vp, ctypes.POINTER(SceneDesc), u32]
     lib.tracer_trace_batched.argtypes = [vp, vp, ctypes.POINTER(TraceParams), u32, i32, vp]
@@ -281,12 +288,13 @@ class Tracer:
     @staticmethod
     def params(width, height, spp=4, max_depth=4, rr_start=0, sky=(0.0, 0.0, 0.0), tie_mode=TIES_STRICT,
                kernel=KERNEL_AUTO, block=0, stack_depth=0, wavefront=0, aovs=(AOV_RGBA8,), stats=False,
-               bvh_width=0) -> TraceParams:
+               bvh_width=0, tail_paths=0) -> TraceParams:
         p = TraceParams()
         p.width, p.height, p.spp, p.max_depth, p.rr_start = width, height, spp, max_depth, rr_start
         p.sky = (ctypes.c_float * 3)(*sky)
         p.tie_mode, p.kernel, p.block, p.stack_depth, p.wavefront = tie_mode, kernel, block, stack_depth, wavefront
         p.bvh_width = bvh_width
+        p.tail_paths = tail_paths
         m = 0
         for a in aovs:
             m |= 1 << a
@@ -379,6 +387,17 @@ class Tracer:
         t = Timings()
         self._check(self.lib.tracer_last_timings(self.h, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in Timings._fields_}
+
+    def rounds(self) -> np.ndarray:
+        """Per-round live paths and kernel times of the last profiled wavefront
+        trace (structured array: paths, finish, extend_ms, shade_ms)."""
+        n = ctypes.c_uint32()
+        self._check(self.lib.tracer_last_rounds(self.h, None, 0, ctypes.byref(n)))
+        buf = (RoundInfo * max(n.value, 1))()
+        self._check(self.lib.tracer_last_rounds(self.h, buf, n.value, ctypes.byref(n)))
+        dt = np.dtype([("paths", np.uint32), ("finish", np.uint32), ("extend_ms", np.float32),
+                       ("shade_ms", np.float32)])
+        return np.frombuffer(bytes(buf), dt, count=n.value).copy()
 
     def device_image(self, aov: int):
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
