@@ -164,6 +164,23 @@ def cpu_baseline_sample(wl, tri_bvh, seconds_target: float = 15.0):
                                      f"{wl.spp} spp), {dt:.1f} s, {rays} rays"
 
 
+def tail_summary(rounds, tail_paths: int) -> dict | None:
+    """Where the profiled frame handed its last paths to the finishing
+    kernel, and what the rounds before cost."""
+    if rounds is None or len(rounds) == 0:
+        return None
+    fin = rounds["finish"] == 1
+    out = {"tail_paths": "auto (extend kernel's resident threads)" if tail_paths == 0 else tail_paths,
+           "rounds": int((~fin).sum()), "first_round_paths": int(rounds["paths"][0])}
+    if fin.any():
+        out["handover_paths"] = int(rounds["paths"][-1])
+        out["finish_ms"] = float(rounds["extend_ms"][-1])
+    full = rounds["paths"][~fin] >= rounds["paths"][0] // 2
+    out["ms_in_rounds_with_half_the_paths_or_more"] = float(
+        (rounds["extend_ms"][~fin][full] + rounds["shade_ms"][~fin][full]).sum())
+    return out
+
+
 def batched_section(local: int, steps: int, warmup: int) -> dict:
     """c2: 64 scenes (triangles log-uniform in [1k, 200k], c1 geometry,
     resolutions from {128^2 .. 1024^2}, 4 spp, depth 6) traced (a) by the plain
@@ -642,7 +659,7 @@ def run_ours(args):
     sptr = stream.cuda_stream
     kern = abi.KERNEL_WAVEFRONT if args.kernel == "wavefront" else abi.KERNEL_PLAIN
     common = dict(spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start, sky=wl.sky, kernel=kern,
-                  block=args.block, wavefront=args.wavefront, bvh_width=args.bvh_width)
+                  block=args.block, wavefront=args.wavefront, bvh_width=args.bvh_width, tail_paths=args.tail_paths)
     p_run = abi.Tracer.params(wl.width, wl.height, aovs=(abi.AOV_RGBA8,), stats=False, **common)
     # counting pass (untimed) with the plain kernel, whose node-visiting order
     # is the oracle's: the canonical ray / node / primitive counts of the frame.
@@ -688,6 +705,7 @@ def run_ours(args):
     flush.zero_()
     tr.trace(wl.frame, p_run, sptr)
     breakdown = tr.timings()
+    rounds = tr.rounds() if kern == abi.KERNEL_WAVEFRONT else None
     tr.set_profiling(False)
 
     # end to end through the C ABI with host buffers
@@ -709,12 +727,15 @@ def run_ours(args):
 
     if rank == 0:
         peak, peak_kind = peaks()
+        l2_gbs = tr.measure_l2_read(32 << 20, 64)
         ab = algorithmic_bytes(st, wl.pixels, 4)
         # dominant kernel: the traversal (extend) kernel of the wavefront, one
         # launch per round; its algorithmic bytes are the traversal bytes of
         # the frame, its time the sum of its launches (CUDA events)
+        # (the finishing kernel traces the last ~1 % of the rays: its time
+        # is counted with the extend launches')
         if kern == abi.KERNEL_WAVEFRONT and breakdown["extend_ms"] > 0:
-            k_ms = breakdown["extend_ms"]
+            k_ms = breakdown["extend_ms"] + breakdown["finish_ms"]
             k_bytes = ab - 4 * wl.pixels
         else:
             k_ms, k_bytes = ms, ab
@@ -739,12 +760,16 @@ def run_ours(args):
                          "frac": achieved / peak,
                          "traffic": (NCU_EXTEND_DRAM_BYTES_PER_RAY * rays
                                      if kern == abi.KERNEL_WAVEFRONT else None),
-                         "kernel": "wf_extend_bvh" if kern == abi.KERNEL_WAVEFRONT else "k_plain",
+                         "kernel": ("wf_extend_bvh (+ wf_finish for the last paths)" if kern == abi.KERNEL_WAVEFRONT
+                                    else "k_plain"),
                          "algorithmic_bytes_per_frame": k_bytes, "kernel_ms_per_frame": k_ms,
                          "launches_per_frame": breakdown["rounds"] if kern == abi.KERNEL_WAVEFRONT else 1,
                          "peak_source": peak_kind,
+                         "l2": {"peak": l2_gbs, "frac": achieved / l2_gbs,
+                                "peak_source": "measured here: reads of a 32 MiB L2-resident buffer, L1 bypassed"},
                          "note": "scene is L2-resident; algorithmic bytes are served mostly by L1/L2"},
             "breakdown": breakdown,
+            "tail": tail_summary(rounds, args.tail_paths),
             "clocks": clocks,
             "gpu_launches": args.steps * int(breakdown["launches"]),
         }
@@ -775,6 +800,8 @@ def main():
     ap.add_argument("--wavefront", type=int, default=0)
     ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4],
                     help="wavefront traversal: 0 auto (4-wide), 2 binary, 4 4-wide")
+    ap.add_argument("--tail-paths", type=int, default=0,
+                    help="wavefront hand-over to the finishing kernel below this many live paths (0 auto, 1 never)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched section")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")

@@ -477,6 +477,13 @@ void tracer_camera_keys(tracer_camera_controller* cam, uint32_t keys, float dt);
 int tracer_camera_script(tracer_camera_controller* cam, const tracer_input_frame* inputs, uint32_t n,
                          tracer_frame* frames_out);
 
+/* ------------------------------------------------------------ measurement
+ * No counterpart in the reference.  Read bandwidth of an L2-resident buffer of
+ * `bytes` (read `passes` times per launch with loads that bypass L1), in GB/s
+ * of bytes delivered: the denominator for kernels whose working set lives in
+ * L2.  Allocates and frees its buffer; synchronous. */
+int tracer_measure_l2_read(tracer_ctx* ctx, size_t bytes, uint32_t passes, double* gbs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,3 +63,12 @@ def test_no_scene():
         with pytest.raises(abi.TracerError) as e:
             tr.trace(S.reference_frame(0.5), abi.Tracer.params(8, 8))
         assert e.value.status == abi.ERR_NO_SCENE
+
+
+def test_measure_l2_read(gpu_tracer):
+    """The L2 read-bandwidth probe: rejects malformed sizes, returns a rate."""
+    for nbytes, passes in ((0, 1), (15, 1), (1 << 20, 0), ((1 << 20) + 8, 4)):
+        with pytest.raises(abi.TracerError):
+            gpu_tracer.measure_l2_read(nbytes, passes)
+    gbs = gpu_tracer.measure_l2_read(8 << 20, 16)
+    assert 100.0 < gbs < 1e6

@@ -774,6 +774,41 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     return TRACER_OK;
 }
 
+int tracer_measure_l2_read(tracer_ctx* c, size_t bytes, uint32_t passes, double* gbs)
+{
+    if (!c || !gbs || passes == 0 || bytes < 16 || bytes % 16) return TRACER_ERR_INVALID_ARG;
+    *gbs = 0.0;
+    cudaSetDevice(c->device);
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    const uint32_t blocks = (uint32_t)c->sm_count * 8;
+    DevBuf<unsigned char> buf;
+    DevBuf<uint32_t> sink;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = dalloc(buf, bytes);
+    if (e == cudaSuccess) e = dalloc(sink, (size_t)blocks * 256);
+    if (e == cudaSuccess) e = cudaMemsetAsync(buf.p, 1, bytes, c->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    // one untimed launch brings the buffer into L2
+    if (e == cudaSuccess) e = launch_l2_read(buf.p, bytes, 1, sink.p, blocks, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], c->stream);
+    if (e == cudaSuccess) e = launch_l2_read(buf.p, bytes, passes, sink.p, blocks, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->stream);
+    if (e == cudaSuccess) {
+        r = wait_event(c, ev[1]);
+        float ms = 0.0f;
+        if (r == TRACER_OK) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        if (r == TRACER_OK && e == cudaSuccess && ms > 0.0f) *gbs = (double)bytes * passes / (ms * 1e-3) / 1e9;
+    }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    buf.release();
+    sink.release();
+    if (e != cudaSuccess) return cuda_fail(c, e, "L2 read measurement");
+    return r;
+}
+
 int tracer_set_profiling(tracer_ctx* c, int enable)
 {
     if (!c) return TRACER_ERR_INVALID_ARG;

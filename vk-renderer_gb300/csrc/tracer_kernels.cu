@@ -59,6 +59,31 @@ static cudaError_t launch_s(const TraceArgs& a, const LaunchConfig& lc, cudaStre
     return lc.stats ? launch_t<TIE, BVH, true>(a, lc, s) : launch_t<TIE, BVH, false>(a, lc, s);
 }
 
+// Reads n 16-byte words `passes` times with loads that are cached in L2 only
+// (ld.global.cg), so a buffer smaller than L2 is served by L2 after the first
+// pass; one word per thread is written so the loads are not optimised away.
+__global__ void __launch_bounds__(256) k_l2_read(const uint4* __restrict__ buf, size_t n, uint32_t passes,
+                                                 uint32_t* __restrict__ sink)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t acc = 0;
+    for (uint32_t p = 0; p < passes; ++p) {
+        for (size_t i = tid; i < n; i += stride) {
+            const uint4 v = __ldcg(buf + i);
+            acc ^= v.x ^ v.y ^ v.z ^ v.w;
+        }
+    }
+    sink[tid] = acc;
+}
+
+cudaError_t launch_l2_read(const void* buf, size_t bytes, uint32_t passes, uint32_t* sink, uint32_t blocks,
+                           cudaStream_t s)
+{
+    k_l2_read<<<blocks, 256, 0, s>>>(static_cast<const uint4*>(buf), bytes / 16, passes, sink);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_plain(const TraceArgs& a, const LaunchConfig& lc, cudaStream_t s)
 {
     if (lc.tie == TIE_REFERENCE) return launch_s<TIE_REFERENCE, false>(a, lc, s);

@@ -40,5 +40,9 @@ struct AdjWf {
 cudaError_t wf_launch_adj_generate(const TraceArgs& a, const WfState& s, const AdjWf& w, cudaStream_t st);
 cudaError_t wf_launch_adj_shade(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
                                 cudaStream_t st);
+// L2 read-bandwidth probe: reads bytes (a multiple of 16) passes times;
+// sink holds blocks * 256 words.
+cudaError_t launch_l2_read(const void* buf, size_t bytes, uint32_t passes, uint32_t* sink, uint32_t blocks,
+                           cudaStream_t s);
 
 }  // namespace vkt

@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = [
     "tracer_readback_scene", "tracer_trace_adjoint", "tracer_present", "tracer_draw", "tracer_draw_reset",
     "tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update", "tracer_camera_move",
     "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script", "tracer_trace_whitted",
-    "tracer_last_rounds",
+    "tracer_last_rounds", "tracer_measure_l2_read",
 ]
 PRESENT_PINGPONG, PRESENT_ACCUMULATE = 0, 1
 KEY_W, KEY_S, KEY_A, KEY_D, KEY_R, KEY_F = 1, 2, 4, 8, 16, 32
@@ -137,6 +137,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_set_profiling.argtypes = [vp, i32]
     lib.tracer_last_timings.argtypes = [vp, ctypes.POINTER(Timings)]
     lib.tracer_last_rounds.argtypes = [vp, ctypes.POINTER(RoundInfo), u32, ctypes.POINTER(u32)]
+    lib.tracer_measure_l2_read.argtypes = [vp, sz, u32, ctypes.POINTER(ctypes.c_double)]
     lib.tracer_trace_noalloc.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp, vp, vp]
     lib.tracer_upload_scenes.argtypes = [vp, ctypes.POINTER(SceneDesc), u32]
     lib.tracer_trace_batched.argtypes = [vp, vp, ctypes.POINTER(TraceParams), u32, i32, vp]
@@ -387,6 +388,12 @@ class Tracer:
         t = Timings()
         self._check(self.lib.tracer_last_timings(self.h, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in Timings._fields_}
+
+    def measure_l2_read(self, nbytes: int = 16 << 20, passes: int = 64) -> float:
+        """Read bandwidth (GB/s) of an L2-resident buffer, loads bypassing L1."""
+        g = ctypes.c_double()
+        self._check(self.lib.tracer_measure_l2_read(self.h, nbytes, passes, ctypes.byref(g)))
+        return g.value
 
     def rounds(self) -> np.ndarray:
         """Per-round live paths and kernel times of the last profiled wavefront
