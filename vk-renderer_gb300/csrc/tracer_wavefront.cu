@@ -9,10 +9,12 @@
 //                next ray from the queue as soon as its ray is finished
 //                (warp-aggregated fetch: ballot + popc + one atomicAdd).
 //                BVH traversal is the speculative while-while scheme: all
-//                lanes step through interior nodes together, postponing the
-//                first leaf each finds, then all test their leaves together;
-//                stacks live in shared memory.  Small register footprint, so
-//                many warps per SM hide the L1/L2 latency of node fetches.
+//                lanes step through interior nodes together, each holding
+//                back up to four leaves it finds, then all test their held
+//                leaves together, one primitive per lane and step; stacks
+//                and held leaves live in shared memory.  Small register
+//                footprint, so many warps per SM hide the L1/L2 latency of
+//                node fetches.
 //   wf_shade     one thread per queued path: the rest of the depth iteration
 //                (:441-549: clamp, sky, scatter, next-event estimation, Russian
 //                roulette).  A surviving path appends itself to the next queue
@@ -112,7 +114,7 @@ struct Lane {
     Hit h;
     const float4* nodes;  // BVH of the current pass
     const float4* prims;  // its primitives (triangles or sphere centres/radii)
-    int cur, leaf, sp, pass;
+    int cur, sp, pass;  // cur: node pair to visit (> 0), leaf (< 0) or none (0)
     uint32_t pid, scene, steps;
     bool has;
 };
@@ -214,34 +216,79 @@ __device__ __forceinline__ void visit_wide(Lane& L, int w, const PairStack& stk,
     L.cur = r0 ? r0 : pop(L, stk);
 }
 
+// Leaves a lane may hold back while the warp's slowest lane is still looking
+// for its first (measured on c1: 2 -> 95.8 ms, 4 -> 91.0, 6 -> 91.0, 8 -> 91.2).
+constexpr int kPostpone = 4;
+
+// Moves leaf references from L.cur into the lane's buffer of postponed leaves
+// (entry j at lbuf[j * stride]), taking the next stack entry after each,
+// until L.cur is an interior node or empty or the buffer is full.
+__device__ __forceinline__ void postpone_leaves(Lane& L, const PairStack& stk, int* lbuf, int stride, int& nl)
+{
+    while (L.cur < 0 && nl < kPostpone) {
+        lbuf[nl * stride] = L.cur;
+        ++nl;
+        L.cur = pop(L, stk);
+    }
+}
+
 template <bool STATS, bool WIDE>
 __device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters& cnt, const PairStack& stk,
-                                           int* status)
+                                           int* lbuf, int stride, int& nl, int* status)
 {
     L.prims = L.pass == 0 ? sc.tri : sc.sph_geo;
-    L.leaf = 0;
     L.sp = 0;
     if (WIDE) {
         L.nodes = L.pass == 0 ? sc.tri_wide : sc.sph_wide;
         visit_wide<STATS>(L, 0, stk, status, cnt);
-        if (L.cur < 0) {
-            L.leaf = L.cur;
-            L.cur = pop(L, stk);
-        }
-        return;
+    } else {
+        L.nodes = L.pass == 0 ? sc.tri_enc : sc.sph_enc;  // references pre-encoded in bmin.w
+        const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
+        if (STATS) cnt.c[C_NODES]++;
+        float tn;
+        L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? __float_as_int(lo.w) : 0;  // the root may be a leaf
     }
-    L.nodes = L.pass == 0 ? sc.tri_enc : sc.sph_enc;  // references pre-encoded in bmin.w
-    const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
-    if (STATS) cnt.c[C_NODES]++;
-    float tn;
-    L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? __float_as_int(lo.w) : 0;
-    if (L.cur < 0) {  // the root is a leaf
-        L.leaf = L.cur;
-        L.cur = 0;
+    postpone_leaves(L, stk, lbuf, stride, nl);
+}
+
+// Tests primitive `slot` of the current pass for the lane's ray.
+template <bool STATS, bool MULTI>
+__device__ __forceinline__ void test_prim(const TraceArgs& a, const TraceArgs* slots, Lane& L, const Ray& ray,
+                                          int slot, Counters& cnt)
+{
+    if (L.pass == 0) {
+        if (STATS) cnt.c[C_TRIS]++;
+        const float4* t = L.prims + 3 * (size_t)slot;
+        const float4 ta = __ldg(t), tb = __ldg(t + 1), tc = __ldg(t + 2);
+        const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
+        const uint32_t id = __float_as_uint(tb.w);
+        if (accept_strict(tt, id, L.h)) {
+            L.h.t = tt;
+            L.h.prim = id;
+            L.h.kind = 1;
+            L.h.slot = slot;
+        }
+    } else {
+        const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
+        if (STATS) cnt.c[C_SPHERES]++;
+        const float4 gg = __ldg(L.prims + slot);
+        const float tt = sphere_intersect(ray, v3(gg), gg.w);
+        const uint32_t id = sc.nt + __ldg(sc.sph_id + slot);
+        if (accept_strict(tt, id, L.h)) {
+            L.h.t = tt;
+            L.h.prim = id;
+            L.h.kind = 2;
+            L.h.slot = slot;
+        }
     }
 }
 
-// 1024 resident threads per SM (64 registers).
+// 1024 resident threads per SM (64 registers).  Each outer iteration: idle
+// lanes fetch rays; all lanes step through interior nodes until every lane
+// still tracing holds a leaf, lanes that already hold some keep going (up to
+// kPostpone leaves, speculatively: their best hit is not yet updated by
+// them); then all lanes test their held leaves' primitives, one primitive per
+// lane and iteration.
 template <int TIE, bool STATS, bool MULTI, int BLOCK, bool WIDE>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     wf_extend_bvh(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
@@ -250,6 +297,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const PairStack stk{reinterpret_cast<int2*>(smem) + threadIdx.x, BLOCK, (int)a.stack_depth};
+    int* lbuf = smem + 2 * (size_t)a.stack_depth * BLOCK + threadIdx.x;  // postponed leaves, stride BLOCK
     const uint32_t total = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
@@ -258,6 +306,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
     Lane L;
     L.has = false;
+    int nl = 0;  // postponed leaves held
     bool exhausted = false;
     for (;;) {
         // 1) idle lanes take the next rays of the queue
@@ -297,7 +346,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     } else {
                         L.br = make_boxray(Ray{L.o, L.d});
                         L.pass = has_tri ? 0 : 1;
-                        start_pass<STATS, WIDE>(sc, L, cnt, stk, a.status);
+                        start_pass<STATS, WIDE>(sc, L, cnt, stk, lbuf, BLOCK, nl, a.status);
                     }
                 }
             }
@@ -306,23 +355,17 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
             if (__all_sync(full, exhausted)) break;
             continue;
         }
-        // 2) interior nodes, until every searching lane has found a leaf
+        // 2) interior nodes, until every lane still tracing holds a leaf
         for (;;) {
-            const bool can = L.has && L.cur > 0;
-            const bool searching = can && L.leaf == 0;
-            if (!__any_sync(full, searching)) break;
+            const bool can = L.has && L.cur > 0 && nl < kPostpone;
+            if (!__any_sync(full, can && nl == 0)) break;
             if (can) {
                 if (++L.steps > a.trav_limit) {
                     atomicCAS(a.status, ST_OK, ST_TRAVERSAL_LIMIT);
                     L.cur = 0;
-                    L.leaf = 0;
                     L.sp = 0;
                 } else if (WIDE) {
                     visit_wide<STATS>(L, L.cur, stk, a.status, cnt);
-                    if (L.cur < 0 && L.leaf == 0) {
-                        L.leaf = L.cur;
-                        L.cur = pop(L, stk);
-                    }
                 } else {
                     const float4* c = L.nodes + 2 * (size_t)L.cur;
                     const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
@@ -338,64 +381,36 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                         L.cur = swap ? e1 : e0;
                         if (h0 && h1) push(L, stk, swap ? e0 : e1, swap ? t0 : t1, a.status);
                     }
-                    if (L.cur < 0 && L.leaf == 0) {
-                        L.leaf = L.cur;
-                        L.cur = pop(L, stk);
+                }
+                postpone_leaves(L, stk, lbuf, BLOCK, nl);
+            }
+        }
+        // 3) the held leaves, one primitive per lane and iteration
+        {
+            int lj = 0, lfirst = 0, lcount = 0;
+            const Ray ray{L.o, L.d};
+            for (;;) {
+                const bool lf = L.has && (lcount > 0 || lj < nl);
+                if (!__any_sync(full, lf)) break;
+                if (lf) {
+                    if (lcount == 0) {
+                        leaf_dec(lbuf[lj * BLOCK], lfirst, lcount);
+                        ++lj;
                     }
+                    test_prim<STATS, MULTI>(a, slots, L, ray, lfirst, cnt);
+                    ++lfirst;
+                    --lcount;
                 }
             }
         }
-        // 3) leaves
-        for (;;) {
-            const bool lf = L.has && L.leaf < 0;
-            if (!__any_sync(full, lf)) break;
-            if (lf) {
-                int first, count;
-                leaf_dec(L.leaf, first, count);
-                const Ray ray{L.o, L.d};
-                if (L.pass == 0) {
-                    for (int k = 0; k < count; ++k) {
-                        if (STATS) cnt.c[C_TRIS]++;
-                        const float4* t = L.prims + 3 * (size_t)(first + k);
-                        const float4 ta = __ldg(t), tb = __ldg(t + 1), tc = __ldg(t + 2);
-                        const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
-                        const uint32_t id = __float_as_uint(tb.w);
-                        if (accept_strict(tt, id, L.h)) {
-                            L.h.t = tt;
-                            L.h.prim = id;
-                            L.h.kind = 1;
-                            L.h.slot = first + k;
-                        }
-                    }
-                } else {
-                    const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
-                    for (int k = 0; k < count; ++k) {
-                        if (STATS) cnt.c[C_SPHERES]++;
-                        const float4 gg = __ldg(L.prims + first + k);
-                        const float tt = sphere_intersect(ray, v3(gg), gg.w);
-                        const uint32_t id = sc.nt + __ldg(sc.sph_id + first + k);
-                        if (accept_strict(tt, id, L.h)) {
-                            L.h.t = tt;
-                            L.h.prim = id;
-                            L.h.kind = 2;
-                            L.h.slot = first + k;
-                        }
-                    }
-                }
-                if (L.cur < 0) {
-                    L.leaf = L.cur;
-                    L.cur = pop(L, stk);
-                } else {
-                    L.leaf = 0;
-                }
-            }
-        }
+        nl = 0;
+        if (L.has) postpone_leaves(L, stk, lbuf, BLOCK, nl);  // a leaf met with the buffer full
         // 4) finished passes: next primitive kind, or planes and the result
-        if (L.has && L.cur == 0 && L.leaf == 0) {
+        if (L.has && L.cur == 0 && nl == 0) {
             const DevScene& sc = SCENE_ARGS(MULTI, a, slots, L.scene).sc;
             if (L.pass == 0 && sc.n_sph_nodes > 0 && sc.ns > 0) {
                 L.pass = 1;
-                start_pass<STATS, WIDE>(sc, L, cnt, stk, a.status);
+                start_pass<STATS, WIDE>(sc, L, cnt, stk, lbuf, BLOCK, nl, a.status);
             } else {
                 planes_pass<STATS>(sc, Ray{L.o, L.d}, L.h, cnt);
                 if (STATS && L.h.kind) cnt.c[C_HITS]++;
@@ -602,11 +617,18 @@ static void smem_attr(K k, size_t smem)
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// Dynamic shared memory of the extend kernel: every thread's traversal stack
+// (8 B per entry) and postponed-leaf buffer (4 B per entry).
+static size_t wf_extend_smem(size_t stack_depth, uint32_t block)
+{
+    return (stack_depth * 8 + kPostpone * 4) * block;
+}
+
 template <int TIE, bool STATS, bool MULTI, int BLOCK>
 static cudaError_t extend_bvh_b(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
     auto k = c.wide ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true> : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
-    const size_t smem = (size_t)a.stack_depth * BLOCK * 8;
+    const size_t smem = wf_extend_smem(a.stack_depth, BLOCK);
     smem_attr(k, smem);
     k<<<c.extend_grid, BLOCK, smem, st>>>(a, s, qsel, c.slots);
     return cudaGetLastError();
@@ -717,7 +739,7 @@ template <int TIE, bool STATS, bool MULTI>
 static int occ_bvh(uint32_t block, size_t stack_depth, bool wide)
 {
     int n = 0;
-    const size_t smem = stack_depth * block * 8;
+    const size_t smem = wf_extend_smem(stack_depth, block);
     cudaError_t e;
     if (block == 64)
         e = occ_bvh_b<TIE, STATS, MULTI, 64>(n, wide, smem);
