@@ -168,19 +168,24 @@ def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case):
     img, lin = _render(tr, sc, fr, p, base)
     _, dl = _loss_and_dl(img, target)
     out = {}
-    for k in (abi.KERNEL_PLAIN, abi.KERNEL_WAVEFRONT):
+    # wavefront: rounds to the end (tail 1), the finishing kernel from the
+    # first read-back on (tail 2^32 - 1), and a hand-over part-way (700)
+    for k, tail in ((abi.KERNEL_PLAIN, 0), (abi.KERNEL_WAVEFRONT, 1), (abi.KERNEL_WAVEFRONT, 0xFFFFFFFF),
+                    (abi.KERNEL_WAVEFRONT, 700)):
         p.kernel = k
+        p.tail_paths = tail
         ga, ge, gc = tr.trace_adjoint(fr, p, dl, lin, num_materials=len(base))
-        out[k] = (ga, ge, gc, tr.stats())
-    pa, pe, pc, ps = out[abi.KERNEL_PLAIN]
-    wa, we, wc, ws = out[abi.KERNEL_WAVEFRONT]
-    assert ps["closest_rays"] == ws["closest_rays"] and ps["hits"] == ws["hits"]
-    assert ps["shadow_rays"] == ws["shadow_rays"] == 0
-    assert np.all(wc == 0.0) and np.all(pc == 0.0)
-    for a, b in ((pa, wa), (pe, we)):
-        scale = float(np.max(np.abs(a))) if np.any(a) else 1.0
-        np.testing.assert_allclose(b, a, rtol=1e-5, atol=1e-7 * scale)
-    assert np.any(wa != 0)
+        out[(k, tail)] = (ga, ge, gc, tr.stats())
+    pa, pe, pc, ps = out[(abi.KERNEL_PLAIN, 0)]
+    for key in ((abi.KERNEL_WAVEFRONT, 1), (abi.KERNEL_WAVEFRONT, 0xFFFFFFFF), (abi.KERNEL_WAVEFRONT, 700)):
+        wa, we, wc, ws = out[key]
+        assert ps["closest_rays"] == ws["closest_rays"] and ps["hits"] == ws["hits"], key
+        assert ps["shadow_rays"] == ws["shadow_rays"] == 0
+        assert np.all(wc == 0.0) and np.all(pc == 0.0)
+        for a, b in ((pa, wa), (pe, we)):
+            scale = float(np.max(np.abs(a))) if np.any(a) else 1.0
+            np.testing.assert_allclose(b, a, rtol=1e-5, atol=1e-7 * scale, err_msg=str(key))
+        assert np.any(wa != 0)
 
 
 def _nee_scene(kind):

@@ -279,8 +279,8 @@ cudaEvent_t prof_event(tracer_ctx* c, size_t i)
 // tail: 0 = the extend kernel's resident threads (below one path per lane, a
 // round costs about the latency of its slowest ray, whatever its size),
 // 1 = never.
-// With adj, the adjoint's generate and shade stages run instead of the
-// forward's (a.linear = the forward image), and there is no finishing kernel.
+// With adj, the adjoint's generate, shade and finishing stages run instead of
+// the forward's (a.linear = the forward image).
 int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots, uint64_t max_rounds,
                   uint32_t stack, uint32_t wavefront, uint32_t tail, cudaStream_t st, const AdjWf* adj = nullptr)
 {
@@ -293,7 +293,7 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     const size_t sg = (nslots + 255) / 256;
     wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
     if (tail == 0) tail = wc.extend_grid * wc.block;
-    const int fin_per = (adj || tail <= 1) ? 0 : wf_finish_blocks_per_sm(wc, stack);
+    const int fin_per = tail <= 1 ? 0 : adj ? wf_adj_finish_blocks_per_sm(a, wc) : wf_finish_blocks_per_sm(wc, stack);
     if (fin_per <= 0) tail = 0;
     cudaError_t e = cudaSuccess;
     if (c->profiling) {
@@ -347,7 +347,7 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
                     c->last_round_entries = (uint32_t)(f + 1);
                     cudaEventRecord(prof_event(c, 3 * f), st);
                 }
-                e = wf_launch_finish(a, ws, wc, fq, st);
+                e = adj ? wf_launch_adj_finish(a, ws, *adj, wc, fq, st) : wf_launch_finish(a, ws, wc, fq, st);
                 if (c->profiling) cudaEventRecord(prof_event(c, 3 * f + 1), st);
                 c->last_launches += 1;
                 c->last_finish = true;
@@ -1679,7 +1679,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         c->last_launches = 1;  // + generate, rounds; the FP64-to-float conversion
         if (c->profiling) cudaEventRecord(c->prof_begin, st);
         // a sample takes at most max_depth rounds in each pass
-        r = run_wavefront(c, a, wc, npx, 2 * (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, 1, st, &aw);
+        r = run_wavefront(c, a, wc, npx, 2 * (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, p->tail_paths, st, &aw);
         if (r != TRACER_OK) return r;
     } else {
         c->last_kernel = 3;

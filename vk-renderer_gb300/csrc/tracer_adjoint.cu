@@ -481,20 +481,161 @@ __device__ __forceinline__ void albedo_grad(double* gal, int m, V3 delta, V3 R, 
     if (albedo.z != 0.0f) gadd(gal, 3 * m + 2, delta.z * R.z / albedo.z);
 }
 
+// One path of the wavefront adjoint between rounds, unpacked (the per-pixel
+// delta and the two saved RNG states stay in memory: pix, prim0).
+struct AdjPath {
+    Ray ray;
+    V3 acc, mask, T;
+    int lc[3];
+    uint32_t sample, depth;
+    bool replay;
+    Rng g;
+};
+
+__device__ __forceinline__ void adj_load(const WfState& s, const TraceArgs& a, uint32_t pid, uint32_t x, uint32_t y,
+                                         AdjPath& p)
+{
+    const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
+    const float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
+    const uint32_t bits = __float_as_uint(accum4.w);
+    p.replay = (bits & kPhaseReplay) != 0;
+    p.sample = (bits >> 16) & 0x7FFFu;
+    p.depth = bits & 0xFFFFu;
+    lc_unpack(__float_as_uint(mask4.w), p.lc);
+    p.g.salt = acc4.w;
+    p.g.cx = (float)x / (float)a.width;
+    p.g.cy = (float)y / (float)a.height;
+    p.ray = Ray{v3(ro), v3(rd)};
+    p.acc = v3(acc4);
+    p.mask = v3(mask4);
+    p.T = v3(accum4);
+}
+
+__device__ __forceinline__ void adj_store(const WfState& s, uint32_t pid, const AdjPath& p)
+{
+    s.ray_o[pid] = make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, depth_tmax(p.depth));
+    s.ray_d[pid] = make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, 0.0f);
+    s.acc[pid] = make_float4(p.acc.x, p.acc.y, p.acc.z, p.g.salt);
+    s.mask[pid] = make_float4(p.mask.x, p.mask.y, p.mask.z, __uint_as_float(lc_pack(p.lc)));
+    s.accum[pid] = make_float4(p.T.x, p.T.y, p.T.z,
+                               __uint_as_float((p.replay ? kPhaseReplay : 0u) | (p.sample << 16) | p.depth));
+}
+
+// One bounce of whichever pass the path is in, given the closest hit h of
+// its ray, then the bookkeeping: pass 1 ends -> pass 2 of the same sample
+// from the sample's first ray and RNG state; pass 2 ends -> the next sample
+// (the RNG continues where pass 1 left it).  pix: the pixel's delta and the
+// RNG salt at the sample's start; prim0: the salt at the end of pass 1.
+// Returns true while the pixel has a ray to trace.
+template <class TR>
+__device__ __forceinline__ bool adj_advance(TR& tr, const TraceArgs& a, const AdjWf& w, uint32_t x, uint32_t y,
+                                            const Hit& h, AdjPath& p, float4* pix, uint32_t* prim0)
+{
+    double* gal = w.grad;
+    double* gem = w.grad + 3 * (size_t)w.nm;
+    const bool found = h.kind != 0;
+    if (!p.replay) {
+        // pass 1: clamp bookkeeping, then the forward bounce
+        if (p.acc.x < 0.0f || p.acc.x > 1.0f) { p.lc[0] = (int)p.depth; p.T.x = 0.0f; }
+        if (p.acc.y < 0.0f || p.acc.y > 1.0f) { p.lc[1] = (int)p.depth; p.T.y = 0.0f; }
+        if (p.acc.z < 0.0f || p.acc.z > 1.0f) { p.lc[2] = (int)p.depth; p.T.z = 0.0f; }
+        p.acc = vclamp01(p.acc);
+        const V3 before = p.acc;
+        const bool cont = shade_bounce(tr, a, p.depth, found, h, p.ray, p.acc, p.mask, p.g);
+        p.T = p.T + (p.acc - before);
+        p.depth++;
+        if (cont && p.depth < a.max_depth) return true;
+        // pass 2 of the same sample: its first ray and RNG state again
+        *prim0 = __float_as_uint(p.g.salt);
+        p.g.salt = pix->w;
+        p.ray = primary_ray(a, x, y);
+        p.acc = splat(0.0f);
+        p.mask = splat(1.0f);
+        p.depth = 0;
+        p.replay = true;
+        return true;
+    }
+    // pass 2: the same bounce, with its gradient terms
+    const V3 delta = v3(*pix);
+    const V3 surv = v3((int)p.depth >= p.lc[0] ? 1.0f : 0.0f, (int)p.depth >= p.lc[1] ? 1.0f : 0.0f,
+                       (int)p.depth >= p.lc[2] ? 1.0f : 0.0f);
+    const V3 wgt = delta * surv;
+    bool cont = false;
+    if (found) {
+        V3 P, N;
+        Material mat;
+        tr.surface(p.ray, h, P, N, mat);
+        const int m = h.kind == 1 ? (int)__float_as_uint(__ldg(a.sc.tri + 3 * (size_t)h.slot).w) : -1;
+        if (mat.type == MAT_DIFFUSE) {
+            const float r2 = rand01(p.g);
+            const V3 d = jitter(N, (2.0f * PI) * rand01(p.g), sqrtf(r2), sqrtf(1.0f - r2)) * (1.0f - mat.metalness);
+            const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
+            const V3 en = emits ? normalize(mat.emissive) : splat(0.0f);
+            if (m >= 0 && emits) {  // d normalize(e) = (I - n n^T) / |e|
+                const V3 wm = wgt * p.mask;
+                const V3 ge = (wm - en * dot(en, wm)) * (1.0f / length(mat.emissive));
+                gadd(gem, 3 * m + 0, ge.x);
+                gadd(gem, 3 * m + 1, ge.y);
+                gadd(gem, 3 * m + 2, ge.z);
+            }
+            p.acc = p.acc + p.mask * en * surv;
+            if (m >= 0) albedo_grad(gal, m, delta, p.T - p.acc, mat.albedo);
+            p.mask = p.mask * mat.albedo;
+            p.ray = Ray{P, normalize(reflect(p.ray.d, N) + d)};
+        } else if (mat.type == MAT_DIELECTRIC) {
+            if (m >= 0) {
+                const V3 ge = wgt * p.mask;
+                gadd(gem, 3 * m + 0, ge.x);
+                gadd(gem, 3 * m + 1, ge.y);
+                gadd(gem, 3 * m + 2, ge.z);
+            }
+            p.acc = p.acc + mat.emissive * p.mask * surv;
+            if (m >= 0) albedo_grad(gal, m, delta, p.T - p.acc, mat.albedo);
+            p.mask = p.mask * mat.albedo;
+            const float cosine = -dot(p.ray.d, N) / length(p.ray.d);
+            const V3 reflected = reflect(p.ray.d, N);
+            const V3 refracted = refract(p.ray.d, N, mat.roughness);
+            const float prob = (refracted == splat(0.0f)) ? 1.0f : schlick(cosine, mat.roughness);
+            p.ray = Ray{P, normalize(rand01(p.g) < prob ? reflected : refracted)};
+        }
+        cont = true;
+        if (p.depth >= a.rr_start) {
+            const float q = max3(p.mask);
+            if (rand01(p.g) > q)
+                cont = false;
+            else
+                p.mask = p.mask * (1.0f / q);
+        }
+    }
+    p.depth++;
+    if (cont && p.depth < a.max_depth) return true;
+    // sample finished: the RNG continues where pass 1 left it
+    p.g.salt = __uint_as_float(*prim0);
+    p.sample++;
+    if (p.sample >= a.spp) return false;
+    p.ray = primary_ray(a, x, y);
+    p.acc = splat(0.0f);
+    p.mask = splat(1.0f);
+    p.T = splat(0.0f);
+    p.lc[0] = p.lc[1] = p.lc[2] = -1;
+    p.depth = 0;
+    p.replay = false;
+    pix->w = p.g.salt;  // the new sample's start
+    return true;
+}
+
 template <int TIE, bool BVH>
 __global__ void __launch_bounds__(256) wf_adj_shade(TraceArgs a, WfState s, AdjWf w, int qsel)
 {
     const uint32_t n = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
     uint32_t* next = qsel ? s.queue[0] : s.queue[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // extend's fetch cursor for the next round
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[2] = 0;  // fetch cursor of the next round
     Counters cnt;
 #pragma unroll
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
     // no emitters: shading traces no shadow rays and needs no stack
     Tracer<TIE, BVH, false> tr{a.sc, Stack{nullptr, nullptr, 0, 0}, cnt, a.status, a.trav_limit};
-    double* gal = w.grad;
-    double* gem = w.grad + 3 * (size_t)w.nm;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t qi = base + threadIdx.x;
@@ -503,136 +644,52 @@ __global__ void __launch_bounds__(256) wf_adj_shade(TraceArgs a, WfState s, AdjW
         if (qi < n) {
             pid = queue[qi];
             const uint32_t x = pid % a.width, y = pid / a.width;
-            const float4 ro = s.ray_o[pid], rd = s.ray_d[pid];
+            AdjPath p;
+            adj_load(s, a, pid, x, y, p);
             const uint4 hr = s.hit[pid];
-            const float4 acc4 = s.acc[pid], mask4 = s.mask[pid], accum4 = s.accum[pid];
-            const uint32_t bits = __float_as_uint(accum4.w);
-            bool replay = (bits & kPhaseReplay) != 0;
-            uint32_t sample = (bits >> 16) & 0x7FFFu, depth = bits & 0xFFFFu;
-            int lc[3];
-            lc_unpack(__float_as_uint(mask4.w), lc);
-            Rng g;
-            g.salt = acc4.w;
-            g.cx = (float)x / (float)a.width;
-            g.cy = (float)y / (float)a.height;
             Hit h;
             h.t = __uint_as_float(hr.x);
             h.prim = hr.y;
             h.slot = hr.z;
             h.kind = (int)hr.w;
-            const bool found = h.kind != 0;
-            Ray ray{v3(ro), v3(rd)};
-            V3 acc = v3(acc4), mask = v3(mask4), T = v3(accum4);
-            float start_salt = 0.0f;
-            bool pix_dirty = false;
-            if (!replay) {
-                // pass 1: clamp bookkeeping, then the forward bounce
-                if (acc.x < 0.0f || acc.x > 1.0f) { lc[0] = (int)depth; T.x = 0.0f; }
-                if (acc.y < 0.0f || acc.y > 1.0f) { lc[1] = (int)depth; T.y = 0.0f; }
-                if (acc.z < 0.0f || acc.z > 1.0f) { lc[2] = (int)depth; T.z = 0.0f; }
-                acc = vclamp01(acc);
-                const V3 before = acc;
-                const bool cont = shade_bounce(tr, a, depth, found, h, ray, acc, mask, g);
-                T = T + (acc - before);
-                depth++;
-                if (cont && depth < a.max_depth) {
-                    again = true;
-                } else {  // pass 2 of the same sample: its first ray and RNG state again
-                    s.prim0[pid] = __float_as_uint(g.salt);
-                    g.salt = w.pix[pid].w;
-                    ray = primary_ray(a, x, y);
-                    acc = splat(0.0f);
-                    mask = splat(1.0f);
-                    depth = 0;
-                    replay = true;
-                    again = true;
-                }
-            } else {
-                // pass 2: the same bounce, with its gradient terms
-                const V3 delta = v3(w.pix[pid]);
-                const V3 surv = v3((int)depth >= lc[0] ? 1.0f : 0.0f, (int)depth >= lc[1] ? 1.0f : 0.0f,
-                                   (int)depth >= lc[2] ? 1.0f : 0.0f);
-                const V3 wgt = delta * surv;
-                bool cont = false;
-                if (found) {
-                    V3 P, N;
-                    Material mat;
-                    tr.surface(ray, h, P, N, mat);
-                    const int m = h.kind == 1 ? (int)__float_as_uint(__ldg(a.sc.tri + 3 * (size_t)h.slot).w) : -1;
-                    if (mat.type == MAT_DIFFUSE) {
-                        const float r2 = rand01(g);
-                        const V3 d = jitter(N, (2.0f * PI) * rand01(g), sqrtf(r2), sqrtf(1.0f - r2)) *
-                                     (1.0f - mat.metalness);
-                        const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
-                        const V3 en = emits ? normalize(mat.emissive) : splat(0.0f);
-                        if (m >= 0 && emits) {  // d normalize(e) = (I - n n^T) / |e|
-                            const V3 wm = wgt * mask;
-                            const V3 ge = (wm - en * dot(en, wm)) * (1.0f / length(mat.emissive));
-                            gadd(gem, 3 * m + 0, ge.x);
-                            gadd(gem, 3 * m + 1, ge.y);
-                            gadd(gem, 3 * m + 2, ge.z);
-                        }
-                        acc = acc + mask * en * surv;
-                        if (m >= 0) albedo_grad(gal, m, delta, T - acc, mat.albedo);
-                        mask = mask * mat.albedo;
-                        ray = Ray{P, normalize(reflect(ray.d, N) + d)};
-                    } else if (mat.type == MAT_DIELECTRIC) {
-                        if (m >= 0) {
-                            const V3 ge = wgt * mask;
-                            gadd(gem, 3 * m + 0, ge.x);
-                            gadd(gem, 3 * m + 1, ge.y);
-                            gadd(gem, 3 * m + 2, ge.z);
-                        }
-                        acc = acc + mat.emissive * mask * surv;
-                        if (m >= 0) albedo_grad(gal, m, delta, T - acc, mat.albedo);
-                        mask = mask * mat.albedo;
-                        const float cosine = -dot(ray.d, N) / length(ray.d);
-                        const V3 reflected = reflect(ray.d, N);
-                        const V3 refracted = refract(ray.d, N, mat.roughness);
-                        const float prob = (refracted == splat(0.0f)) ? 1.0f : schlick(cosine, mat.roughness);
-                        ray = Ray{P, normalize(rand01(g) < prob ? reflected : refracted)};
-                    }
-                    cont = true;
-                    if (depth >= a.rr_start) {
-                        const float p = max3(mask);
-                        if (rand01(g) > p)
-                            cont = false;
-                        else
-                            mask = mask * (1.0f / p);
-                    }
-                }
-                depth++;
-                if (cont && depth < a.max_depth) {
-                    again = true;
-                } else {  // sample finished: the RNG continues where pass 1 left it
-                    g.salt = __uint_as_float(s.prim0[pid]);
-                    sample++;
-                    if (sample < a.spp) {
-                        ray = primary_ray(a, x, y);
-                        acc = splat(0.0f);
-                        mask = splat(1.0f);
-                        T = splat(0.0f);
-                        lc[0] = lc[1] = lc[2] = -1;
-                        depth = 0;
-                        replay = false;
-                        start_salt = g.salt;
-                        pix_dirty = true;
-                        again = true;
-                    }
-                }
-            }
-            if (again) {
-                s.ray_o[pid] = make_float4(ray.o.x, ray.o.y, ray.o.z, depth_tmax(depth));
-                s.ray_d[pid] = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
-                s.acc[pid] = make_float4(acc.x, acc.y, acc.z, g.salt);
-                s.mask[pid] = make_float4(mask.x, mask.y, mask.z, __uint_as_float(lc_pack(lc)));
-                s.accum[pid] = make_float4(T.x, T.y, T.z,
-                                           __uint_as_float((replay ? kPhaseReplay : 0u) | (sample << 16) | depth));
-                if (pix_dirty) w.pix[pid].w = start_salt;
-            }
+            again = adj_advance(tr, a, w, x, y, h, p, w.pix + pid, s.prim0 + pid);
+            if (again) adj_store(s, pid, p);
         }
         warp_append(again, pid, next, &s.count[qsel ^ 1]);
     }
+}
+
+// The adjoint's finishing kernel (as wf_finish for the forward): each thread
+// runs queued paths to the end of their pixels -- both passes of every
+// remaining sample -- with the per-thread traversal for the closest hits.
+template <int TIE, bool BVH, bool STATS>
+__global__ void __launch_bounds__(128) wf_adj_finish(TraceArgs a, WfState s, AdjWf w, int qsel)
+{
+    extern __shared__ int smem[];
+    const uint32_t n = s.count[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
+                    (int)blockDim.x, (int)a.stack_depth};
+    Tracer<TIE, BVH, STATS> tr{a.sc, stk, cnt, a.status, a.trav_limit};
+    const uint32_t threads = gridDim.x * blockDim.x;
+    uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    while (qi < n) {
+        const uint32_t pid = queue[qi];
+        const uint32_t x = pid % a.width, y = pid / a.width;
+        AdjPath p;
+        adj_load(s, a, pid, x, y, p);
+        for (;;) {
+            Hit h;
+            h.t = depth_tmax(p.depth);
+            tr.trace(p.ray, h, false);
+            if (!adj_advance(tr, a, w, x, y, h, p, w.pix + pid, s.prim0 + pid)) break;
+        }
+        qi = n > threads ? threads + atomicAdd(&s.count[2], 1u) : n;
+    }
+    if (STATS) flush_counters(a, cnt);
 }
 
 cudaError_t wf_launch_adj_generate(const TraceArgs& a, const WfState& s, const AdjWf& w, cudaStream_t st)
@@ -652,6 +709,61 @@ cudaError_t wf_launch_adj_shade(const TraceArgs& a, const WfState& s, const AdjW
     else
         wf_adj_shade<TIE_STRICT, false><<<c.shade_grid, 256, 0, st>>>(a, s, w, qsel);
     return cudaGetLastError();
+}
+
+template <int TIE, bool BVH, bool STATS>
+static size_t adj_finish_smem(const TraceArgs& a)
+{
+    const size_t smem = BVH ? (size_t)a.stack_depth * 128 * 8 : 0;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(wf_adj_finish<TIE, BVH, STATS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return smem;
+}
+
+template <int TIE, bool BVH, bool STATS>
+static cudaError_t adj_finish_t(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
+                                cudaStream_t st)
+{
+    wf_adj_finish<TIE, BVH, STATS><<<c.finish_grid, 128, adj_finish_smem<TIE, BVH, STATS>(a), st>>>(a, s, w, qsel);
+    return cudaGetLastError();
+}
+
+template <int TIE, bool BVH, bool STATS>
+static int adj_finish_occ(const TraceArgs& a)
+{
+    int n = 0;
+    const size_t smem = adj_finish_smem<TIE, BVH, STATS>(a);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_adj_finish<TIE, BVH, STATS>, 128, smem) == cudaSuccess
+               ? n
+               : 0;
+}
+
+template <bool STATS>
+static cudaError_t adj_finish_s(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
+                                cudaStream_t st)
+{
+    if (c.tie == TIE_REFERENCE) return adj_finish_t<TIE_REFERENCE, false, STATS>(a, s, w, c, qsel, st);
+    if (c.bvh) return adj_finish_t<TIE_STRICT, true, STATS>(a, s, w, c, qsel, st);
+    return adj_finish_t<TIE_STRICT, false, STATS>(a, s, w, c, qsel, st);
+}
+
+template <bool STATS>
+static int adj_finish_occ_s(const TraceArgs& a, const WfConfig& c)
+{
+    if (c.tie == TIE_REFERENCE) return adj_finish_occ<TIE_REFERENCE, false, STATS>(a);
+    if (c.bvh) return adj_finish_occ<TIE_STRICT, true, STATS>(a);
+    return adj_finish_occ<TIE_STRICT, false, STATS>(a);
+}
+
+cudaError_t wf_launch_adj_finish(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
+                                 cudaStream_t st)
+{
+    return c.stats ? adj_finish_s<true>(a, s, w, c, qsel, st) : adj_finish_s<false>(a, s, w, c, qsel, st);
+}
+
+int wf_adj_finish_blocks_per_sm(const TraceArgs& a, const WfConfig& c)
+{
+    return c.stats ? adj_finish_occ_s<true>(a, c) : adj_finish_occ_s<false>(a, c);
 }
 
 template <int TIE, bool BVH, bool CAM>

@@ -40,6 +40,11 @@ struct AdjWf {
 cudaError_t wf_launch_adj_generate(const TraceArgs& a, const WfState& s, const AdjWf& w, cudaStream_t st);
 cudaError_t wf_launch_adj_shade(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
                                 cudaStream_t st);
+// The adjoint's finishing kernel: every path of queue qsel to the end of its
+// pixel (c.finish_grid blocks of 128 threads; the cursor count[2] starts at 0).
+cudaError_t wf_launch_adj_finish(const TraceArgs& a, const WfState& s, const AdjWf& w, const WfConfig& c, int qsel,
+                                 cudaStream_t st);
+int wf_adj_finish_blocks_per_sm(const TraceArgs& a, const WfConfig& c);
 // L2 read-bandwidth probe: reads bytes (a multiple of 16) passes times;
 // sink holds blocks * 256 words.
 cudaError_t launch_l2_read(const void* buf, size_t bytes, uint32_t passes, uint32_t* sink, uint32_t blocks,
