@@ -662,12 +662,14 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
     // AUTO: the wavefront pays for itself on BVH scenes with enough path
     // bounces in flight; the plain kernel wins on linear-scan scenes and small
-    // frames (the reference's own 10-primitive frame: 1.6 ms plain against
-    // 2.2 ms wavefront; 512^2 x 1 spp x depth 2: 0.07 against 0.11 ms;
-    // 1920x1080 x 16 spp x depth 8: 225 against 100 ms)
+    // frames.  Measured (plain / wavefront ms): the reference's own 10-primitive
+    // frame 1.6 / 2.2; c1 scene 256^2 x 4 spp x depth 8 (2^21 bounces)
+    // 2.98 / 3.26, 512x288 x 4 x 8 (4.7M) 5.74 / 3.98, 1920x1080 x 16 x 8
+    // 225 / 91; c3 scene 256^2 x 4 x 4 (2^20) 0.59 / 0.90, 512^2 x 4 x 4
+    // (2^22) 1.44 / 1.20; c0 512^2 x 1 x 2 0.067 / 0.118.
     const uint64_t bounces = (uint64_t)p->width * p->height * p->spp * p->max_depth;
     const int kernel = p->kernel != TRACER_KERNEL_AUTO ? p->kernel
-                       : (c->scene.bvh && bounces >= (1ull << 24)) ? TRACER_KERNEL_WAVEFRONT
+                       : (c->scene.bvh && bounces >= (1ull << 22)) ? TRACER_KERNEL_WAVEFRONT
                                                                    : TRACER_KERNEL_PLAIN;
     if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
