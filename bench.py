@@ -318,7 +318,7 @@ def adjoint_section(local: int, steps: int) -> dict:
     ms_fwd = timed(lambda: tr.trace(wl.frame, p_run, sptr))
     adj = lambda: tr.trace_adjoint(wl.frame, p_run, dl_d.data_ptr(), lin_d.data_ptr(),
                                    outputs=(ga.data_ptr(), ge.data_ptr(), gc.data_ptr()), stream=sptr)
-    ms_adj = timed(adj)  # AUTO: the per-pixel kernel below 2^17 pixels, else the wavefront
+    ms_adj = timed(adj)  # AUTO: the wavefront (c3 has no emissive spheres)
     adj_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
     # both adjoint forms on the same inputs, for comparison
     per_kernel = {}
@@ -362,7 +362,7 @@ def adjoint_section(local: int, steps: int) -> dict:
     return {"metric": "adjoint Mrays/s (c3, path replay)", "value": adjv, "unit": UNIT, "ms_per_step": ms_adj,
             "forward": {"value": fwd, "ms_per_step": ms_fwd, "rays_per_step": fwd_rays},
             "adjoint_rays_per_step": adj_rays, "ratio_adjoint_to_forward": adjv / fwd,
-            "kernel": "auto (" + ("wavefront" if wl.width * wl.height >= 1 << 17 else "per-pixel") + ")",
+            "kernel": "auto (wavefront: no emissive spheres)",
             "kernels": per_kernel,
             "forward_rays_per_adjoint_second_ratio": ms_fwd / ms_adj,
             "grad_check": {"max_rel_err_vs_central_fd": max(rel), "step": 1e-3,

@@ -1587,13 +1587,11 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         return fail(c, TRACER_ERR_STACK_OVERFLOW, "stack depth %u below the BVH depth %u", stack, need);
     if ((size_t)stack * 128 * 8 > 100 * 1024)
         return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
-    // AUTO: below ~128k pixels the wavefront's per-round launches cost more
-    // than the per-pixel kernel's divergence (256^2 x 4 spp: 2.8 ms against
-    // 1.8 ms; 1024^2 x 64 spp: 5.8x faster as a wavefront)
-    const size_t npx_all = (size_t)p->width * p->height;
-    const int kernel = p->kernel == TRACER_KERNEL_AUTO
-                           ? (npx_all >= (1u << 17) ? TRACER_KERNEL_WAVEFRONT : TRACER_KERNEL_PLAIN)
-                           : p->kernel;
+    // AUTO: the wavefront wherever it applies (below).  With its finishing
+    // kernel it is the faster form at every size measured on the c3 scene
+    // (per-pixel / wavefront ms): 64^2 x 4 spp 1.29 / 1.25, 128^2 1.30 / 1.13,
+    // 256^2 1.72 / 1.36, 512^2 4.65 / 2.48; 1024^2 x 64 spp: 5.8x.
+    const int kernel = p->kernel == TRACER_KERNEL_AUTO ? TRACER_KERNEL_WAVEFRONT : p->kernel;
     if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
     const uint32_t wblock = p->block ? p->block : 128;
