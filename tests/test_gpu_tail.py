@@ -166,3 +166,25 @@ def test_graph_handover_replayed_for_other_frames(gpu_tracer):
         want = [tr.readback_scene(i, abi.AOV_RGBA32F).copy() for i in range(len(scenes))]
         for i in range(len(scenes)):
             assert np.array_equal(fbits(got[i]), fbits(want[i])), (shift, i)
+
+
+def test_auto_kernel_choice(gpu_tracer):
+    """TRACER_KERNEL_AUTO: the wavefront (rounds > 0) for BVH scenes from 2^22
+    pixel x spp x depth, else the plain kernel; linear-scan scenes plain."""
+    sc = soup_scene(5, 4000, extent=12.0, sigma=0.5)
+    fr = S.frame(S.look_at((0.0, 3.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.7)
+    gpu_tracer.set_profiling(True)
+    try:
+        for bvh, (w, h, spp, depth), wavefront in ((True, (256, 256, 4, 4), False), (True, (512, 512, 4, 4), True),
+                                                   (False, (512, 512, 4, 4), False)):
+            if bvh:
+                gpu_tracer.upload_scene(sc)
+            else:
+                gpu_tracer.upload_scene(S.Scene(triangles=sc.triangles[:200], materials=sc.materials,
+                                                bvh=S.BVH_NONE))
+            p = abi.Tracer.params(w, h, spp=spp, max_depth=depth, rr_start=2, sky=(1.0, 1.0, 1.0),
+                                  kernel=abi.KERNEL_AUTO)
+            gpu_tracer.trace(fr, p)
+            assert (gpu_tracer.timings()["rounds"] > 0) == wavefront, (bvh, w, h, spp, depth)
+    finally:
+        gpu_tracer.set_profiling(False)
