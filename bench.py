@@ -226,10 +226,12 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
     ms_plain = timed(p_plain, False)
     plain_imgs = [tr.readback_scene(k, abi.AOV_RGBA32F) for k in range(len(wls))]
     p_wf = prm(abi.KERNEL_WAVEFRONT, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F))
-    best, table = tune.autotune_batched(tr, frames, p_wf, budget_s=40.0)
+    # binary traversal only (4-wide measured slower on these soups); the
+    # finishing kernel's threshold: the library's choice or 1M live paths
+    best, table = tune.autotune_batched(tr, frames, p_wf, widths=(2,), tails=(0, 1_000_000), budget_s=40.0)
     for p in p_wf:
         p.block, p.stack_depth, p.wavefront = best["block"], best["stack_depth"], best["wavefront"]
-        p.bvh_width = best["bvh_width"]
+        p.bvh_width, p.tail_paths = best["bvh_width"], best["tail_paths"]
     ms_wf = timed(p_wf, True)
     rmse = 0.0
     for k in range(len(wls)):

@@ -120,11 +120,13 @@ def test_timings_after_graph_and_autotune(gpu_tracer):
         assert t["extend_ms"] > 0 and t["shade_ms"] > 0
     finally:
         tr.set_profiling(False)
-    best, table = tune.autotune_batched(tr, frames, params, blocks=(64, 128), stacks=(4, 32), wavefronts=(0, 2))
+    best, table = tune.autotune_batched(tr, frames, params, blocks=(64, 128), stacks=(4, 32), wavefronts=(0, 2),
+                                        tails=(0, 1))
     assert best is not None and best["ms"] > 0
     assert any("skipped" in r for r in table)  # stack 4 is below the BVH depth
-    assert len(table) == 16  # widths 4 and 2
-    assert best["bvh_width"] in (2, 4)
+    assert len(table) == 32  # widths 4 and 2, tails auto and never
+    assert best["bvh_width"] in (2, 4) and best["tail_paths"] in (0, 1)
+    assert all(p.tail_paths == 0 for p in params)  # the parameters are restored
 
 
 def test_batched_argument_errors(gpu_tracer):

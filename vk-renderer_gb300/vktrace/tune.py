@@ -16,28 +16,30 @@ import time
 from . import abi
 
 
-def _set(params, block, stack, wave, width):
+def _set(params, block, stack, wave, width, tail=0):
     for p in params:
-        p.block, p.stack_depth, p.wavefront, p.bvh_width = block, stack, wave, width
+        p.block, p.stack_depth, p.wavefront, p.bvh_width, p.tail_paths = block, stack, wave, width, tail
 
 
 def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stacks=(0, 16, 32, 64),
-                     wavefronts=(0, 6, 4), widths=(4, 2), reps: int = 1, use_graph: bool = True,
+                     wavefronts=(0, 6, 4), widths=(4, 2), tails=(0,), reps: int = 1, use_graph: bool = True,
                      budget_s: float = 60.0):
     """Returns (best, table): best = dict(block, stack_depth, wavefront,
-    bvh_width, ms); table = one dict per candidate (ms or skipped reason)."""
+    bvh_width, tail_paths, ms); table = one dict per candidate (ms or
+    skipped reason).  tails: tail_paths values (live paths below which the
+    rest goes to the finishing kernel; 0 = the library's choice)."""
     table = []
     best = None
     t_start = time.perf_counter()
-    saved = [(p.block, p.stack_depth, p.wavefront, p.bvh_width) for p in params]
+    saved = [(p.block, p.stack_depth, p.wavefront, p.bvh_width, p.tail_paths) for p in params]
     tr.set_profiling(True)
     try:
-        for width, block, stack, wave in itertools.product(widths, blocks, stacks, wavefronts):
-            cand = {"block": block, "stack_depth": stack, "wavefront": wave, "bvh_width": width}
+        for width, block, stack, wave, tail in itertools.product(widths, blocks, stacks, wavefronts, tails):
+            cand = {"block": block, "stack_depth": stack, "wavefront": wave, "bvh_width": width, "tail_paths": tail}
             if time.perf_counter() - t_start > budget_s:
                 table.append(dict(cand, skipped="time budget"))
                 continue
-            _set(params, block, stack, wave, width)
+            _set(params, block, stack, wave, width, tail)
             try:
                 tr.trace_batched(frames, params, use_graph=use_graph)  # first run: graph capture, caches warm
                 tr.synchronize()
@@ -55,8 +57,8 @@ def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stac
                 best = dict(row)
     finally:
         tr.set_profiling(False)
-        for p, (b, s, w, wd) in zip(params, saved):
-            p.block, p.stack_depth, p.wavefront, p.bvh_width = b, s, w, wd
+        for p, (b, s, w, wd, tl) in zip(params, saved):
+            p.block, p.stack_depth, p.wavefront, p.bvh_width, p.tail_paths = b, s, w, wd, tl
     return best, table
 
 
