@@ -541,7 +541,7 @@ __device__ __forceinline__ bool adj_advance(TR& tr, const TraceArgs& a, const Ad
         if (p.acc.z < 0.0f || p.acc.z > 1.0f) { p.lc[2] = (int)p.depth; p.T.z = 0.0f; }
         p.acc = vclamp01(p.acc);
         const V3 before = p.acc;
-        const bool cont = shade_bounce(tr, a, p.depth, found, h, p.ray, p.acc, p.mask, p.g);
+        const bool cont = shade_bounce<false>(tr, a, p.depth, found, h, p.ray, p.acc, p.mask, p.g);  // no emitters
         p.T = p.T + (p.acc - before);
         p.depth++;
         if (cont && p.depth < a.max_depth) return true;

@@ -330,8 +330,9 @@ __device__ __forceinline__ float depth_tmax(uint32_t depth)
 // estimation, Russian roulette.  Updates acc, mask and ray; returns false
 // when the path ends (miss or roulette).  acc must already be clamped
 // (Tracer.comp:441; the clamp does not affect the trace, so it may run before
-// or after it).
-template <class TR>
+// or after it).  NEE = false leaves out the next-event code for scenes
+// without emissive spheres (its loop would run no iteration there).
+template <bool NEE = true, class TR>
 __device__ __forceinline__ bool shade_bounce(TR& tr, const TraceArgs& a, uint32_t depth, bool found, const Hit& h,
                                              Ray& ray, V3& acc, V3& mask, Rng& g)
 {
@@ -346,7 +347,8 @@ __device__ __forceinline__ bool shade_bounce(TR& tr, const TraceArgs& a, uint32_
         const float r2 = rand01(g);
         const V3 d = jitter(N, (2.0f * PI) * rand01(g), sqrtf(r2), sqrtf(1.0f - r2)) * (1.0f - mat.metalness);
         V3 e = splat(0.0f);
-        for (uint32_t k = 0; k < a.sc.ne; ++k) e = e + nee_one(tr, a, __ldg(a.sc.emit + k), P, N, mat, g);
+        if (NEE)
+            for (uint32_t k = 0; k < a.sc.ne; ++k) e = e + nee_one(tr, a, __ldg(a.sc.emit + k), P, N, mat, g);
         const bool emits = mat.emissive.x > 0.0f && mat.emissive.y > 0.0f && mat.emissive.z > 0.0f;
         const V3 emissive = emits ? normalize(mat.emissive) : splat(0.0f);
         acc = acc + mask * (emissive + e);

@@ -499,8 +499,8 @@ __device__ __forceinline__ void store_path(const WfState& s, uint32_t pid, const
 // sample and pixel bookkeeping (:578-592): the next depth, else the pixel's
 // next sample (its RNG continues where the last sample stopped), else the
 // resolve.  Returns true while the pixel has another ray to trace: p.ray, with
-// tmax depth_tmax(p.depth).
-template <class TR>
+// tmax depth_tmax(p.depth).  NEE: as shade_bounce.
+template <bool NEE, class TR>
 __device__ __forceinline__ bool advance_path(TR& tr, const TraceArgs& A, uint32_t x, uint32_t y, const Hit& h,
                                              PathRegs& p)
 {
@@ -510,7 +510,7 @@ __device__ __forceinline__ bool advance_path(TR& tr, const TraceArgs& A, uint32_
         p.t0 = found ? h.t : -1.0f;
     }
     p.acc = vclamp01(p.acc);
-    const bool cont = shade_bounce(tr, A, p.depth, found, h, p.ray, p.acc, p.mask, p.g);
+    const bool cont = shade_bounce<NEE>(tr, A, p.depth, found, h, p.ray, p.acc, p.mask, p.g);
     p.depth++;
     if (cont && p.depth < A.max_depth) return true;
     p.accum = p.accum + p.acc;
@@ -527,7 +527,7 @@ __device__ __forceinline__ bool advance_path(TR& tr, const TraceArgs& A, uint32_
 }
 
 // ------------------------------------------------------------------- shade --
-template <int TIE, bool BVH, bool STATS, bool MULTI>
+template <int TIE, bool BVH, bool STATS, bool MULTI, bool NEE>
 __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
     extern __shared__ int smem[];
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
             h.prim = hr.y;
             h.slot = hr.z;
             h.kind = (int)hr.w;
-            again = advance_path(tr, A, x, y, h, ps);
+            again = advance_path<NEE>(tr, A, x, y, h, ps);
             if (again) store_path(s, pid, ps);
         }
         warp_append(again, pid, next, &s.count[qsel ^ 1]);
@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
 // First path of a thread: queue entry = its global index; later ones from the
 // cursor count[2] (zeroed by the shade that wrote the queue), offset by the
 // number of threads.
-template <int TIE, bool BVH, bool STATS, bool MULTI>
+template <int TIE, bool BVH, bool STATS, bool MULTI, bool NEE>
 __global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
     extern __shared__ int smem[];
@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qse
             Hit h;
             h.t = depth_tmax(ps.depth);
             tr.trace(ps.ray, h, false);
-            if (!advance_path(tr, A, x, y, h, ps)) break;
+            if (!advance_path<NEE>(tr, A, x, y, h, ps)) break;
         }
         qi = n > threads ? threads + atomicAdd(&s.count[2], 1u) : n;
     }
@@ -649,7 +649,7 @@ static cudaError_t extend_t(const TraceArgs& a, const WfState& s, const WfConfig
 template <int TIE, bool BVH, bool STATS, bool MULTI>
 static cudaError_t shade_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
-    auto k = wf_shade<TIE, BVH, STATS, MULTI>;
+    auto k = c.has_emitters ? wf_shade<TIE, BVH, STATS, MULTI, true> : wf_shade<TIE, BVH, STATS, MULTI, false>;
     const size_t smem = (BVH && c.has_emitters) ? (size_t)a.stack_depth * 256 * 8 : 0;
     smem_attr(k, smem);
     k<<<c.shade_grid, 256, smem, st>>>(a, s, qsel, c.slots);
@@ -659,7 +659,7 @@ static cudaError_t shade_t(const TraceArgs& a, const WfState& s, const WfConfig&
 template <int TIE, bool BVH, bool STATS, bool MULTI>
 static cudaError_t finish_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
-    auto k = wf_finish<TIE, BVH, STATS, MULTI>;
+    auto k = c.has_emitters ? wf_finish<TIE, BVH, STATS, MULTI, true> : wf_finish<TIE, BVH, STATS, MULTI, false>;
     const size_t smem = BVH ? (size_t)a.stack_depth * 128 * 8 : 0;
     smem_attr(k, smem);
     k<<<c.finish_grid, 128, smem, st>>>(a, s, qsel, c.slots);
@@ -667,9 +667,9 @@ static cudaError_t finish_t(const TraceArgs& a, const WfState& s, const WfConfig
 }
 
 template <int TIE, bool BVH, bool STATS, bool MULTI>
-static int finish_occ(size_t smem)
+static int finish_occ(size_t smem, bool nee)
 {
-    auto k = wf_finish<TIE, BVH, STATS, MULTI>;
+    auto k = nee ? wf_finish<TIE, BVH, STATS, MULTI, true> : wf_finish<TIE, BVH, STATS, MULTI, false>;
     smem_attr(k, smem);
     int n = 0;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 128, smem) == cudaSuccess ? n : 0;
@@ -718,13 +718,15 @@ cudaError_t wf_launch_finish(const TraceArgs& a, const WfState& s, const WfConfi
 int wf_finish_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
 {
     const size_t smem = c.bvh ? (size_t)stack_depth * 128 * 8 : 0;
-    if (c.multi) return c.stats ? finish_occ<TIE_STRICT, true, true, true>(smem)
-                                : finish_occ<TIE_STRICT, true, false, true>(smem);
-    if (c.tie == TIE_REFERENCE) return c.stats ? finish_occ<TIE_REFERENCE, false, true, false>(smem)
-                                               : finish_occ<TIE_REFERENCE, false, false, false>(smem);
-    if (c.bvh) return c.stats ? finish_occ<TIE_STRICT, true, true, false>(smem)
-                              : finish_occ<TIE_STRICT, true, false, false>(smem);
-    return c.stats ? finish_occ<TIE_STRICT, false, true, false>(smem) : finish_occ<TIE_STRICT, false, false, false>(smem);
+    const bool nee = c.has_emitters != 0;
+    if (c.multi) return c.stats ? finish_occ<TIE_STRICT, true, true, true>(smem, nee)
+                                : finish_occ<TIE_STRICT, true, false, true>(smem, nee);
+    if (c.tie == TIE_REFERENCE) return c.stats ? finish_occ<TIE_REFERENCE, false, true, false>(smem, nee)
+                                               : finish_occ<TIE_REFERENCE, false, false, false>(smem, nee);
+    if (c.bvh) return c.stats ? finish_occ<TIE_STRICT, true, true, false>(smem, nee)
+                              : finish_occ<TIE_STRICT, true, false, false>(smem, nee);
+    return c.stats ? finish_occ<TIE_STRICT, false, true, false>(smem, nee)
+                   : finish_occ<TIE_STRICT, false, false, false>(smem, nee);
 }
 
 template <int TIE, bool STATS, bool MULTI, int BLOCK>
