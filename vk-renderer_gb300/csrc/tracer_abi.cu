@@ -1475,8 +1475,8 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
                 // runs whatever paths are queued after that round.
                 r = run_wavefront(c, a, wc, total, max_rounds, stack, p0.wavefront, p0.tail_paths, st);
                 if (r != TRACER_OK) return r;
-                const uint64_t rounds = c->last_handover ? c->last_handover : max_rounds;
                 const int fin_per = c->last_handover ? wf_finish_blocks_per_sm(wc, stack) : 0;
+                const uint64_t rounds = fin_per > 0 ? c->last_handover : max_rounds;
                 c->graph_rounds = rounds;
                 c->graph_finish = fin_per > 0;
                 cudaStream_t cap;
