@@ -168,8 +168,8 @@ def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case):
     img, lin = _render(tr, sc, fr, p, base)
     _, dl = _loss_and_dl(img, target)
     out = {}
-    # wavefront: rounds to the end (tail 1), the finishing kernel from the
-    # first read-back on (tail 2^32 - 1), and a hand-over part-way (700)
+    # wavefront: rounds to the end (tail 1), the finishing kernel right after
+    # generate (tail 2^32 - 1), and a hand-over part-way (700)
     for k, tail in ((abi.KERNEL_PLAIN, 0), (abi.KERNEL_WAVEFRONT, 1), (abi.KERNEL_WAVEFRONT, 0xFFFFFFFF),
                     (abi.KERNEL_WAVEFRONT, 700)):
         p.kernel = k

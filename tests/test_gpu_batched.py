@@ -110,6 +110,8 @@ def test_timings_after_graph_and_autotune(gpu_tracer):
     tr = gpu_tracer
     scenes, frames, params = _batch()
     tr.upload_scenes(scenes)
+    for p in params:
+        p.tail_paths = 1  # rounds to the end (this small batch would otherwise run no round)
     tr.set_profiling(True)
     try:
         tr.trace_batched(frames, params, use_graph=True)
@@ -120,6 +122,8 @@ def test_timings_after_graph_and_autotune(gpu_tracer):
         assert t["extend_ms"] > 0 and t["shade_ms"] > 0
     finally:
         tr.set_profiling(False)
+    for p in params:
+        p.tail_paths = 0
     best, table = tune.autotune_batched(tr, frames, params, blocks=(64, 128), stacks=(4, 32), wavefronts=(0, 2),
                                         tails=(0, 1))
     assert best is not None and best["ms"] > 0

@@ -14,7 +14,7 @@ from vktrace import scene as S
 pytestmark = pytest.mark.gpu
 
 NEVER = 1  # no path count is below 1 while paths remain
-ALWAYS = 0xFFFFFFFF  # hand over as soon as the first count is read back
+ALWAYS = 0xFFFFFFFF  # more than any frame's pixels: no round, the finishing kernel after generate
 
 
 def _same(a, b, what):
@@ -94,7 +94,7 @@ def test_round_statistics(gpu_tracer):
             gpu_tracer.trace(fr, p)
             r = gpu_tracer.rounds()
             t = gpu_tracer.timings()
-            assert len(r) >= 2
+            assert len(r) >= 1
             assert r["paths"][0] == 64 * 64
             assert np.all(np.diff(r["paths"].astype(np.int64)) <= 0)
             assert np.all(r["extend_ms"] > 0)
@@ -108,13 +108,14 @@ def test_round_statistics(gpu_tracer):
             else:
                 assert fin[-1] and fin.sum() == 1
                 assert r["shade_ms"][-1] == 0.0 and t["finish_ms"] > 0.0
-                # the count that triggered the hand-over is read three rounds late
                 f = len(r) - 1
-                assert r["paths"][f - 3] < tail
-                if f >= 5:
-                    assert r["paths"][f - 4] >= tail
                 if tail == ALWAYS:
-                    assert f == 4
+                    assert f == 0  # fewer pixels than the threshold: no round at all
+                else:
+                    # the count that triggered the hand-over is read three rounds late
+                    assert r["paths"][f - 3] < tail
+                    if f >= 5:
+                        assert r["paths"][f - 4] >= tail
             assert t["rounds"] == int((~fin).sum())
     finally:
         gpu_tracer.set_profiling(False)

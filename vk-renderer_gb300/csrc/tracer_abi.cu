@@ -123,7 +123,7 @@ struct tracer_ctx {
     DevBuf<uint32_t> round_paths;   // profiling: live paths at the start of each round (+ the finish)
     uint32_t last_round_entries = 0;
     bool last_finish = false;       // the finishing kernel ran in the last trace
-    uint32_t last_handover = 0;     // rounds before the finishing kernel in the last trace (0: none ran)
+    uint32_t last_handover = 0;     // rounds before the finishing kernel in the last trace (if last_finish)
     int last_kernel = 0;
     // batch of scenes (tracer_upload_scenes / tracer_trace_batched)
     SceneBuffers batch;                 // arena: every scene's arrays back to back
@@ -278,7 +278,9 @@ cudaEvent_t prof_event(tracer_ctx* c, size_t i)
 // grow from round to round, so the lagged count bounds the current one).
 // tail: 0 = the extend kernel's resident threads (below one path per lane, a
 // round costs about the latency of its slowest ray, whatever its size),
-// 1 = never.
+// 1 = never.  With fewer path slots than tail from the start, no round runs:
+// the finishing kernel traces every pixel after generate (c3's 256^2 adjoint:
+// 1.33 ms with four rounds first).
 // With adj, the adjoint's generate, shade and finishing stages run instead of
 // the forward's (a.linear = the forward image).
 int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots, uint64_t max_rounds,
@@ -310,6 +312,24 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
         e = wf_launch_generate(a, ws, wc, st);
     }
     c->last_launches += 1;
+    if (e == cudaSuccess && tail > 1 && nslots < tail) {
+        const uint64_t blocks = ((uint64_t)nslots + 127) / 128;
+        const uint64_t cap = (uint64_t)fin_per * c->sm_count;
+        wc.finish_grid = (uint32_t)(blocks < cap ? blocks : cap);
+        if (c->profiling) {
+            cudaMemcpyAsync(c->round_paths.p, c->wf_count.p, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+            c->last_round_entries = 1;
+            cudaEventRecord(prof_event(c, 0), st);
+        }
+        e = adj ? wf_launch_adj_finish(a, ws, *adj, wc, 0, st) : wf_launch_finish(a, ws, wc, 0, st);
+        if (c->profiling) cudaEventRecord(prof_event(c, 1), st);
+        c->last_launches += 1;
+        c->last_finish = true;
+        c->last_handover = 0;
+        c->last_rounds = 0;
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront launch");
+        return TRACER_OK;
+    }
     for (uint64_t r = 0; r < max_rounds && e == cudaSuccess; ++r) {
         const int qsel = (int)(r & 1);
         if (c->profiling) {
@@ -1475,7 +1495,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
                 // runs whatever paths are queued after that round.
                 r = run_wavefront(c, a, wc, total, max_rounds, stack, p0.wavefront, p0.tail_paths, st);
                 if (r != TRACER_OK) return r;
-                const int fin_per = c->last_handover ? wf_finish_blocks_per_sm(wc, stack) : 0;
+                const int fin_per = c->last_finish ? wf_finish_blocks_per_sm(wc, stack) : 0;
                 const uint64_t rounds = fin_per > 0 ? c->last_handover : max_rounds;
                 c->graph_rounds = rounds;
                 c->graph_finish = fin_per > 0;
