@@ -1,7 +1,7 @@
 """The wavefront's finishing kernel (tracer_trace_params.tail_paths): once few
 paths are live, one launch runs each of them to the end of its pixel.  The
 image, hits and ray counts must not depend on where the hand-over happens:
-never, after the first rounds (every path still live) or part-way through."""
+never, before any round (every path still live) or part-way through."""
 import numpy as np
 import pytest
 
