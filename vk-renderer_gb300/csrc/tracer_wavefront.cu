@@ -571,13 +571,14 @@ __global__ void __launch_bounds__(256) wf_shade(TraceArgs a, WfState s, int qsel
 // Runs every queued path to the end of its pixel in one launch: a thread takes
 // a path and traces and shades it bounce after bounce, sample after sample,
 // with the per-thread traversal, until the pixel is resolved; then it takes
-// the next.  For the last rounds of a wavefront, when few paths are live:
-// they then need no launches per round and do not wait each round for that
-// round's slowest ray.  The operations per pixel are those of extend + shade,
-// in the same order, so the results are identical.
+// the next.  For the last rounds of a wavefront, when few paths are live, and
+// for whole frames with fewer pixels than that: the paths then need no
+// launches per round and do not wait each round for that round's slowest ray.
+// The operations per pixel are those of extend + shade, in the same order, so
+// the results are identical.
 // First path of a thread: queue entry = its global index; later ones from the
-// cursor count[2] (zeroed by the shade that wrote the queue), offset by the
-// number of threads.
+// cursor count[2] (zeroed by the generate or shade that wrote the queue),
+// offset by the number of threads.
 template <int TIE, bool BVH, bool STATS, bool MULTI, bool NEE>
 __global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
 {
