@@ -41,19 +41,10 @@
 #include <cuda_runtime.h>
 
 #include "tracer_core.cuh"
+#include "tracer_traverse.cuh"
 #include "tracer_wavefront.h"
 
 namespace vkt {
-
-// The traversal reads the binary BVH with each record's child reference
-// encoded at upload (bmin.w): interior -> index of its children pair (>= 1),
-// leaf -> -1 - ((first << 6) | (count - 1)).
-__device__ __forceinline__ void leaf_dec(int enc, int& first, int& count)
-{
-    const int v = -1 - enc;
-    first = v >> 6;
-    count = (v & 63) + 1;
-}
 
 // The TraceArgs a path belongs to: the launch's own (single scene) or its
 // scene's entry in the table (batched).
@@ -100,72 +91,6 @@ __global__ void __launch_bounds__(256) wf_generate(TraceArgs a, WfState s, const
 }
 
 // ------------------------------------------------------------------ extend --
-// Strict-tie acceptance without a separate tmax: the running best starts as
-// (t = tmax, prim = 0), so a candidate at exactly tmax fails the id test and
-// every candidate must satisfy t < tmax, as accept<TIE_STRICT> requires.
-__device__ __forceinline__ bool accept_strict(float t, uint32_t id, const Hit& h)
-{
-    return (t > EPSILON) && ((t < h.t) || (t == h.t && id < h.prim));
-}
-
-struct Lane {
-    V3 o, d;
-    BoxRay br;
-    Hit h;
-    const float4* nodes;  // BVH of the current pass
-    const float4* prims;  // its primitives (triangles or sphere centres/radii)
-    int cur, sp, pass;  // cur: node pair to visit (> 0), leaf (< 0) or none (0)
-    uint32_t pid, scene, steps;
-    bool has;
-};
-
-// Planes after the BVHs (unbounded; scanned linearly, Tracer.comp:414-428).
-template <bool STATS>
-__device__ __forceinline__ void planes_pass(const DevScene& sc, const Ray& ray, Hit& h, Counters& cnt)
-{
-    for (uint32_t i = 0; i < sc.np; ++i) {
-        if (STATS) cnt.c[C_PLANES]++;
-        const float4 q = __ldg(sc.planes + 4 * (size_t)i + 3);
-        const float tt = plane_intersect(ray, v3(q), q.w);
-        const uint32_t id = sc.nt + sc.ns + i;
-        if (accept_strict(tt, id, h)) {
-            h.t = tt;
-            h.prim = id;
-            h.kind = 3;
-            h.slot = i;
-        }
-    }
-}
-
-// The traversal stack in shared memory: one 8-byte entry (child reference,
-// entry distance) per level, lanes interleaved (entry k of thread t at
-// k * stride + t), so a push or a pop is one access.
-struct PairStack {
-    int2* e;
-    int stride, cap;
-};
-
-__device__ __forceinline__ int pop(Lane& L, const PairStack& stk)
-{
-    const float limit = L.h.t * BOX_SLACK;
-    while (L.sp > 0) {
-        --L.sp;
-        const int2 v = stk.e[L.sp * stk.stride];
-        if (__int_as_float(v.y) <= limit) return v.x;
-    }
-    return 0;
-}
-
-__device__ __forceinline__ void push(Lane& L, const PairStack& stk, int e, float tn, int* status)
-{
-    if (L.sp >= stk.cap) {
-        atomicCAS(status, ST_OK, ST_STACK_OVERFLOW);
-        return;
-    }
-    stk.e[L.sp * stk.stride] = make_int2(e, __float_as_int(tn));
-    ++L.sp;
-}
-
 __device__ __forceinline__ void order2(float& ta, int& ra, float& tb, int& rb)
 {
     if (tb < ta) {
@@ -590,6 +515,11 @@ __global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qse
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
     const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
                     (int)blockDim.x, (int)a.stack_depth};
+    // the closest-hit traversal's stack (8-byte entries interleaved by thread)
+    // after the shadow rays' (stk: 4-byte entries interleaved by thread, used
+    // only with NEE), so no thread's entries overlap another's
+    const size_t pbase = NEE ? 2 * (size_t)a.stack_depth * blockDim.x : 0;  // in ints
+    const PairStack pstk{reinterpret_cast<int2*>(smem + pbase) + threadIdx.x, (int)blockDim.x, (int)a.stack_depth};
     const uint32_t threads = gridDim.x * blockDim.x;
     uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
     while (qi < n) {
@@ -603,7 +533,10 @@ __global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qse
         for (;;) {
             Hit h;
             h.t = depth_tmax(ps.depth);
-            tr.trace(ps.ray, h, false);
+            if (BVH)
+                closest_enc<STATS>(A.sc, ps.ray, h, pstk, a.status, A.trav_limit, cnt);
+            else
+                tr.trace(ps.ray, h, false);
             if (!advance_path<NEE>(tr, A, x, y, h, ps)) break;
         }
         qi = n > threads ? threads + atomicAdd(&s.count[2], 1u) : n;
@@ -657,11 +590,18 @@ static cudaError_t shade_t(const TraceArgs& a, const WfState& s, const WfConfig&
     return cudaGetLastError();
 }
 
+// Dynamic shared memory of the finishing kernel (128 threads): the closest-hit
+// stack and, with next-event estimation, the shadow rays' stack before it.
+static size_t wf_finish_smem(bool bvh, bool nee, size_t stack_depth)
+{
+    return bvh ? stack_depth * 128 * 8 * (nee ? 2 : 1) : 0;
+}
+
 template <int TIE, bool BVH, bool STATS, bool MULTI>
 static cudaError_t finish_t(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
     auto k = c.has_emitters ? wf_finish<TIE, BVH, STATS, MULTI, true> : wf_finish<TIE, BVH, STATS, MULTI, false>;
-    const size_t smem = BVH ? (size_t)a.stack_depth * 128 * 8 : 0;
+    const size_t smem = wf_finish_smem(BVH, c.has_emitters != 0, a.stack_depth);
     smem_attr(k, smem);
     k<<<c.finish_grid, 128, smem, st>>>(a, s, qsel, c.slots);
     return cudaGetLastError();
@@ -718,8 +658,8 @@ cudaError_t wf_launch_finish(const TraceArgs& a, const WfState& s, const WfConfi
 
 int wf_finish_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
 {
-    const size_t smem = c.bvh ? (size_t)stack_depth * 128 * 8 : 0;
     const bool nee = c.has_emitters != 0;
+    const size_t smem = wf_finish_smem(c.bvh != 0, nee, stack_depth);
     if (c.multi) return c.stats ? finish_occ<TIE_STRICT, true, true, true>(smem, nee)
                                 : finish_occ<TIE_STRICT, true, false, true>(smem, nee);
     if (c.tie == TIE_REFERENCE) return c.stats ? finish_occ<TIE_REFERENCE, false, true, false>(smem, nee)
