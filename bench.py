@@ -170,7 +170,7 @@ def tail_summary(rounds, tail_paths: int) -> dict | None:
     if rounds is None or len(rounds) == 0:
         return None
     fin = rounds["finish"] == 1
-    out = {"tail_paths": "auto (extend kernel's resident threads)" if tail_paths == 0 else tail_paths,
+    out = {"tail_paths": "auto (twice the extend kernel's resident threads)" if tail_paths == 0 else tail_paths,
            "rounds": int((~fin).sum()), "first_round_paths": int(rounds["paths"][0])}
     if fin.any():
         out["handover_paths"] = int(rounds["paths"][-1])

@@ -170,8 +170,9 @@ def test_graph_handover_replayed_for_other_frames(gpu_tracer):
 
 
 def test_auto_kernel_choice(gpu_tracer):
-    """TRACER_KERNEL_AUTO: the wavefront (rounds > 0) for BVH scenes from 2^22
-    pixel x spp x depth, else the plain kernel; linear-scan scenes plain."""
+    """TRACER_KERNEL_AUTO: the wavefront (more than one launch) for BVH scenes
+    from 2^22 pixel x spp x depth, else the plain kernel (one launch);
+    linear-scan scenes plain."""
     sc = soup_scene(5, 4000, extent=12.0, sigma=0.5)
     fr = S.frame(S.look_at((0.0, 3.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.7)
     gpu_tracer.set_profiling(True)
@@ -186,6 +187,6 @@ def test_auto_kernel_choice(gpu_tracer):
             p = abi.Tracer.params(w, h, spp=spp, max_depth=depth, rr_start=2, sky=(1.0, 1.0, 1.0),
                                   kernel=abi.KERNEL_AUTO)
             gpu_tracer.trace(fr, p)
-            assert (gpu_tracer.timings()["rounds"] > 0) == wavefront, (bvh, w, h, spp, depth)
+            assert (gpu_tracer.timings()["launches"] > 1) == wavefront, (bvh, w, h, spp, depth)
     finally:
         gpu_tracer.set_profiling(False)

@@ -276,11 +276,14 @@ cudaEvent_t prof_event(tracer_ctx* c, size_t i)
 // Once a read-back count is below tail, the finishing kernel runs the paths
 // still queued to the end of their pixels and the rounds stop (counts never
 // grow from round to round, so the lagged count bounds the current one).
-// tail: 0 = the extend kernel's resident threads (below one path per lane, a
-// round costs about the latency of its slowest ray, whatever its size),
-// 1 = never.  With fewer path slots than tail from the start, no round runs:
-// the finishing kernel traces every pixel after generate (c3's 256^2 adjoint:
-// 1.33 ms with four rounds first).
+// tail: 0 = twice the extend kernel's resident threads (below about one path
+// per lane a round costs the latency of its slowest ray, whatever its size;
+// measured on c1 with the finishing kernel as built: 1x 89.1 ms, 1.5x 88.6,
+// 2x 88.5), 1 = never.  With fewer path slots than that from the start (for
+// auto: fewer than the resident threads themselves), no round runs: the
+// finishing kernel traces every pixel after generate (c3's 256^2 adjoint:
+// 1.33 ms with four rounds first; a 640x360 frame of c1's scene, 230k
+// pixels: 5.0 ms without rounds against 4.5 with them).
 // With adj, the adjoint's generate, shade and finishing stages run instead of
 // the forward's (a.linear = the forward image).
 int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots, uint64_t max_rounds,
@@ -294,7 +297,9 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     wc.extend_grid = (uint32_t)(per * c->sm_count);
     const size_t sg = (nslots + 255) / 256;
     wc.shade_grid = (uint32_t)(sg < (size_t)c->sm_count * 8 ? sg : (size_t)c->sm_count * 8);
-    if (tail == 0) tail = wc.extend_grid * wc.block;
+    const uint32_t resident = wc.extend_grid * wc.block;
+    const uint32_t no_rounds_below = tail == 0 ? resident : tail;
+    if (tail == 0) tail = 2 * resident;
     const int fin_per = tail <= 1 ? 0 : adj ? wf_adj_finish_blocks_per_sm(a, wc) : wf_finish_blocks_per_sm(wc, stack);
     if (fin_per <= 0) tail = 0;
     cudaError_t e = cudaSuccess;
@@ -312,7 +317,7 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
         e = wf_launch_generate(a, ws, wc, st);
     }
     c->last_launches += 1;
-    if (e == cudaSuccess && tail > 1 && nslots < tail) {
+    if (e == cudaSuccess && tail > 1 && nslots < no_rounds_below) {
         const uint64_t blocks = ((uint64_t)nslots + 127) / 128;
         const uint64_t cap = (uint64_t)fin_per * c->sm_count;
         wc.finish_grid = (uint32_t)(blocks < cap ? blocks : cap);
@@ -1086,7 +1091,7 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     // image is smaller than the extend kernel's resident threads), the
     // finishing kernel traces every pixel in one launch; otherwise every round
     // is launched, and a round with an empty queue returns at once.
-    const uint32_t tail = p->tail_paths ? p->tail_paths : wc.extend_grid * wc.block;
+    const uint32_t tail = p->tail_paths ? p->tail_paths : 2 * wc.extend_grid * wc.block;
     const int fin_per = tail > npx ? wf_finish_blocks_per_sm(wc, stack) : 0;
     if (fin_per > 0) {
         const size_t blocks = (npx + 127) / 128, cap = (size_t)fin_per * c->sm_count;
