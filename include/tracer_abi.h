@@ -205,9 +205,9 @@ typedef struct tracer_trace_params {
                                triangle soups, where it tests boxes the binary traversal culls) */
     uint32_t tail_paths;    /* wavefront: once fewer than this many paths are live, one kernel runs each of
                                them to the end of its pixel (remaining bounces and samples) instead of
-                               further rounds (a frame with fewer pixels runs no round at all); 0 = auto
-                               (twice the extend kernel's resident threads), 1 = never.  Same images either
-                               way. */
+                               further rounds; a frame with fewer pixels than this runs no round at all.
+                               0 = auto: twice the extend kernel's resident threads, no round below once
+                               that; 1 = never.  Same images either way. */
 } tracer_trace_params;
 
 typedef struct tracer_stats {
