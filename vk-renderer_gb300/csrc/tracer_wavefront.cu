@@ -208,7 +208,7 @@ __device__ __forceinline__ void test_prim(const TraceArgs& a, const TraceArgs* s
     }
 }
 
-// 1024 resident threads per SM (64 registers).  Each outer iteration: idle
+// 1024 resident threads per SM (63 registers).  Each outer iteration: idle
 // lanes fetch rays; all lanes step through interior nodes until every lane
 // still tracing holds a leaf, lanes that already hold some keep going (up to
 // kPostpone leaves, speculatively: their best hit is not yet updated by
