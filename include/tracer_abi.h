@@ -230,6 +230,14 @@ const char* tracer_last_error(const tracer_ctx* ctx);
 const char* tracer_status_string(int status);
 /* Bound for every wait on the GPU (default 60000 ms). */
 int tracer_set_timeout(tracer_ctx* ctx, uint32_t timeout_ms);
+/* Cap on the BVH traversal steps of one ray (no counterpart in the
+ * reference, whose linear scan has no such loop).  0 = automatic: twice the
+ * BVH's node count plus 16, which a valid BVH never reaches.  A ray that
+ * reaches the cap ends its traversal with the best hit found so far, the
+ * kernels run to completion, and the next wait reports
+ * TRACER_ERR_TRAVERSAL_LIMIT; the context stays usable.  For exercising that
+ * failure path; applies to every later trace of the context. */
+int tracer_set_traversal_limit(tracer_ctx* ctx, uint32_t steps);
 
 /* Replaces the scene SSBO upload (GraphicsDevice.cpp:796-822).  Copies the
  * arrays to the GPU, building or validating BVHs; replaces any previous scene. */
@@ -334,10 +342,15 @@ int tracer_last_rounds(tracer_ctx* ctx, tracer_round_info* out, uint32_t cap, ui
  * has already allocated.  Such a caller creates the context and uploads the
  * scene once at start-up, then calls this entry point per frame.
  *
- * It runs the wavefront kernels on the scene uploaded to ctx (with no queue
- * length read back: when the image has fewer pixels than tail_paths -- always
- * with the automatic threshold -- the generate kernel and one finishing
- * launch, else every round) and writes the
+ * It runs the wavefront kernels on the scene uploaded to ctx, 128 threads per
+ * block, binary traversal (bvh_width 0 or 2; other widths are refused; the
+ * block field is not read), with no queue length read back: when the image
+ * has fewer pixels than tail_paths -- always with the automatic threshold,
+ * which is the extend kernel's resident threads as in tracer_trace -- the
+ * generate kernel and one finishing launch; otherwise (tail_paths = 1, or a
+ * tail_paths at most the pixel count) every one of the spp * max_depth + 1
+ * rounds is launched (2 kernels each, a round with no live path returning at
+ * once).  It writes the
  * image straight into caller-owned device buffers: rgba8_out (w*h*4 bytes)
  * and/or rgba32f_out (w*h*16 bytes); either may be NULL, not both.  The
  * wavefront's path state, queues and counters live in one fixed array of

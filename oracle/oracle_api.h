@@ -68,6 +68,13 @@ void oracle_accumulate(const float* linear_rgba, float* sum_rgba, uint32_t n_pix
 void oracle_whitted(const float* frame96, uint32_t width, uint32_t height, float* rgba32f, uint8_t* rgba8,
                     oracle_stats* stats);
 
+/* bvh_oracle.cpp: the oracle's own BVH builder (kind 1 = median split, 2 =
+ * binned SAH; prim_type 0 = 48 B triangles, 1 = 64 B spheres), node for node
+ * the product's definition (32 B nodes, children side by side, root 0).
+ * nodes_out: room for 2n - 1 nodes.  Returns 0, or -1 on bad arguments. */
+int oracle_build_bvh(int kind, int prim_type, const void* prims, uint32_t n, uint32_t leaf_size, uint32_t bins,
+                     void* nodes_out, uint32_t* num_nodes, uint32_t* prim_index_out, uint32_t* depth_out);
+
 typedef struct oracle_camera_ctl {
     float cam[16];        /* CameraData: pos, dir, right, up (16-byte lanes) */
     float front[3];

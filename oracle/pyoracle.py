@@ -51,11 +51,28 @@ def build() -> str:
     return LIB
 
 
+def reference_root() -> str:
+    """Where the reference tree is read from: $VKTRACE_REFERENCE_ROOT, else the
+    harness recipe's default (its REF variable)."""
+    env = os.environ.get("VKTRACE_REFERENCE_ROOT")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", os.path.join(HERE, "ref"), "ref-dir"],
+                       capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
+def reference_present() -> bool:
+    root = reference_root()
+    return bool(root) and os.path.isdir(os.path.join(root, "Assets"))
+
+
 def build_ref() -> bool:
     """Builds the reference-shader harness when the reference tree exists."""
-    if not os.path.isdir("/root/reference/Assets"):
+    if not reference_present():
         return False
-    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"OUT={REF_DIR}"], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"OUT={REF_DIR}", f"REF={reference_root()}"],
+                   check=True)
     return True
 
 
@@ -104,6 +121,9 @@ def lib() -> ctypes.CDLL:
                          ("oracle_camera_keyboard", [pc, u32, f32])):
             getattr(L, fn).argtypes = args
             getattr(L, fn).restype = None
+        L.oracle_build_bvh.argtypes = [i32, i32, vp, u32, u32, u32, vp, ctypes.POINTER(u32), vp,
+                                       ctypes.POINTER(u32)]
+        L.oracle_build_bvh.restype = i32
         _lib = L
     return _lib
 
@@ -142,6 +162,29 @@ def params(width, height, spp=4, max_depth=4, rr_start=0, sky=(0.0, 0.0, 0.0), t
     if rows is not None:
         p.row_begin, p.row_end, p.row_step = rows
     return p
+
+
+# 32-byte BVH node record (bmin, left_or_first, bmax, count), as the product's
+NODE = np.dtype({"names": ["bmin", "left_or_first", "bmax", "count"],
+                 "formats": [("<f4", 3), "<i4", ("<f4", 3), "<i4"], "offsets": [0, 12, 16, 28], "itemsize": 32})
+
+
+def build_bvh(kind: int, prims: np.ndarray, leaf_size: int = 0, sah_bins: int = 0):
+    """The oracle's own BVH builder (bvh_oracle.cpp): kind 1 = median split,
+    2 = binned SAH; prims = 48-byte triangle or 64-byte sphere records.
+    Returns (nodes, prim_index, depth) like the product's builder."""
+    L = lib()
+    prims = np.ascontiguousarray(prims)
+    ptype = 0 if prims.dtype.itemsize == 48 else 1
+    n = len(prims)
+    nodes = np.zeros(max(1, 2 * n), NODE)
+    idx = np.zeros(n, np.uint32)
+    nn, depth = ctypes.c_uint32(), ctypes.c_uint32()
+    r = L.oracle_build_bvh(kind, ptype, _p(prims), n, leaf_size, sah_bins, _p(nodes), ctypes.byref(nn), _p(idx),
+                           ctypes.byref(depth))
+    if r != 0:
+        raise ValueError("oracle_build_bvh: bad arguments")
+    return nodes[: nn.value].copy(), idx, depth.value
 
 
 def render(sc, frame, prm: OParams, tri_bvh=None, sphere_bvh=None):

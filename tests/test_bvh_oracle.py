@@ -86,3 +86,32 @@ def test_nan_ray_is_not_traversed(oracle_lib, tracer_lib):
     tb = abi.build_bvh(S.BVH_SAH, tris)[:2]
     r = oracle_lib.trace_ray(sc, (0, 0, 20), (np.nan, np.nan, np.nan), 3000.0, tri_bvh=tb)
     assert not r["found"] and r["stats"]["node_fetches"] == 0 and r["stats"]["closest_rays"] == 1
+
+
+@pytest.mark.parametrize("case", ["c1-soup", "c3-soup", "c0-spheres", "degenerate", "one", "median-tris", "leaf1"])
+def test_oracle_builder_equals_product(oracle_lib, tracer_lib, case):
+    """The oracle builds its BVHs with its own code (so the CPU baseline needs
+    nothing from the product library); node for node, index for index, it
+    must equal the product's builder."""
+    kind, leaf, bins = S.BVH_SAH, 4, 16
+    if case == "c1-soup":
+        prims = configs.c1().scene.triangles
+    elif case == "c3-soup":
+        prims = configs.c3().scene.triangles
+    elif case == "c0-spheres":
+        prims, kind, leaf = configs.c0().scene.spheres, S.BVH_MEDIAN, 2
+    elif case == "degenerate":
+        prims = np.zeros(37, S.TRIANGLE)
+        prims["v1"] = (1, 0, 0)
+        prims["v2"] = (0, 1, 0)
+    elif case == "one":
+        prims = S.triangle_soup(5, 1)[0]
+    elif case == "median-tris":
+        prims, kind, leaf = S.triangle_soup(6, 3000, extent=20.0)[0], S.BVH_MEDIAN, 2
+    else:
+        prims, leaf, bins = S.triangle_soup(7, 2000, extent=5.0, sigma=2.0)[0], 1, 8
+    pn, pi, pd = abi.build_bvh(kind, prims, leaf_size=leaf, sah_bins=bins)
+    on, oi, od = oracle_lib.build_bvh(kind, prims, leaf_size=leaf, sah_bins=bins)
+    assert len(on) == len(pn) and od == pd
+    assert on.tobytes() == pn.tobytes()
+    assert np.array_equal(oi, pi)

@@ -72,3 +72,32 @@ def test_measure_l2_read(gpu_tracer):
             gpu_tracer.measure_l2_read(nbytes, passes)
     gbs = gpu_tracer.measure_l2_read(8 << 20, 16)
     assert 100.0 < gbs < 1e6
+
+
+@pytest.mark.parametrize("kernel,tail", [(abi.KERNEL_PLAIN, 0), (abi.KERNEL_WAVEFRONT, 1),
+                                         (abi.KERNEL_WAVEFRONT, 0)])
+def test_traversal_limit_fires_then_recovers(gpu_tracer, kernel, tail):
+    """The device-side traversal step cap, lowered to a handful of steps,
+    stops rays mid-traversal: the kernels finish, the wait reports
+    TRACER_ERR_TRAVERSAL_LIMIT, and with the automatic cap back the same
+    context traces the frame as before (the plain kernel, the wavefront's
+    rounds, and its finishing kernel)."""
+    tr = gpu_tracer
+    sc = soup_scene(12, 3000, extent=10.0, sigma=0.5)
+    tr.upload_scene(sc)
+    fr = S.frame(S.look_at((0.0, 0.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.5)
+    p = abi.Tracer.params(64, 64, spp=2, max_depth=4, rr_start=3, sky=(1, 1, 1), kernel=kernel, tail_paths=tail,
+                          aovs=(abi.AOV_RGBA32F,))
+    tr.trace(fr, p)
+    ref = tr.readback(abi.AOV_RGBA32F)
+    try:
+        tr.set_traversal_limit(3)
+        tr.trace(fr, p)
+        with pytest.raises(abi.TracerError) as e:
+            tr.synchronize()
+        assert e.value.status == abi.ERR_TRAVERSAL_LIMIT
+    finally:
+        tr.set_traversal_limit(0)
+    tr.trace(fr, p)
+    again = tr.readback(abi.AOV_RGBA32F)
+    assert np.array_equal(np.nan_to_num(again, nan=-7.0), np.nan_to_num(ref, nan=-7.0))

@@ -4,7 +4,6 @@ golden vectors recorded from the reference shader compiled for the host
 host; libm mode is checked only on the host whose C library made the goldens
 (cos in libm is not bit-identical across C libraries / CPUs)."""
 import hashlib
-import os
 
 import numpy as np
 import pytest
@@ -135,7 +134,7 @@ def test_random_triangle_ssbo(oracle_lib, trig):
 def test_live_harness_if_present(oracle_lib):
     """When the reference tree is mounted, compare against the compiled shader
     live on a fresh random scene and camera (not only the committed vectors)."""
-    if not os.path.isdir("/root/reference/Assets"):
+    if not oracle_lib.reference_present():
         pytest.skip("reference tree not mounted")
     oracle_lib.build_ref()
     h = oracle_lib.RefHarness(rng_trig=True)

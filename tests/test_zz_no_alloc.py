@@ -20,19 +20,30 @@ from vktrace import scene as S
 pytestmark = pytest.mark.gpu
 
 
-def _case():
+def _case(emitters=False):
+    if emitters:  # the reference's spheres (one emitter: next-event shadow rays) and planes
+        ref = S.reference_scene()
+        sc = soup_scene(44, 400, extent=30.0, sigma=4.0)
+        sc.spheres, sc.planes = ref.spheres, ref.planes
+        return sc, S.reference_frame(0.35), 100, 80
     sc = soup_scene(21, 2500, extent=10.0, sigma=0.5)
     fr = S.frame(S.look_at((0.0, 2.0, 30.0), (0.0, 0.0, 0.0), 40.0), 120 / 96, 0.75)
     return sc, fr, 120, 96
 
 
-def test_noalloc_matches_regular_trace_twice(gpu_tracer):
+@pytest.mark.parametrize("emitters", [False, True])
+@pytest.mark.parametrize("tail_paths", [0, 1])
+def test_noalloc_matches_regular_trace_twice(gpu_tracer, tail_paths, emitters):
+    """Two calls in a row, each equal to tracer_trace's image: the finishing
+    kernel after generate (tail_paths 0) and every round launched
+    (tail_paths 1), on a triangle soup and on a scene with an emissive sphere
+    and planes."""
     import torch
-    sc, fr, w, h = _case()
+    sc, fr, w, h = _case(emitters)
     tr = gpu_tracer
     tr.upload_scene(sc)
     p = abi.Tracer.params(w, h, spp=3, max_depth=6, rr_start=3, sky=(1.0, 1.0, 1.0),
-                          aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F), kernel=abi.KERNEL_WAVEFRONT)
+                          aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F), kernel=abi.KERNEL_WAVEFRONT, tail_paths=tail_paths)
     tr.trace(fr, p)
     ref8 = tr.readback(abi.AOV_RGBA8)
     ref32 = tr.readback(abi.AOV_RGBA32F)
@@ -51,6 +62,30 @@ def test_noalloc_matches_regular_trace_twice(gpu_tracer):
         assert e <= IMAGE_RMSE_TOL, (call, e)
         assert np.array_equal(got8, ref8), call
         assert np.array_equal(np.isnan(got32[:, 0]), np.isnan(ref32[:, 0]))
+
+
+def test_noalloc_device_memory_unchanged(gpu_tracer):
+    """The property the entry point exists for: once the library's code and
+    its fixed array are resident (a first call), further calls take no device
+    memory -- the device's free memory is the same before and after a run of
+    calls, with both branches (finishing kernel, every round)."""
+    import torch
+    sc, fr, w, h = _case()
+    tr = gpu_tracer
+    tr.upload_scene(sc)
+    out8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+    prm = [abi.Tracer.params(w, h, spp=2, max_depth=4, rr_start=3, sky=(1.0, 1.0, 1.0), tail_paths=t)
+           for t in (0, 1)]
+    for p in prm:  # first calls: module code and kernels loaded
+        tr.trace_noalloc(fr, p, out8.data_ptr(), None)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        for p in prm:
+            tr.trace_noalloc(fr, p, out8.data_ptr(), None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_single_output_and_limits(gpu_tracer):
@@ -76,3 +111,9 @@ def test_noalloc_single_output_and_limits(gpu_tracer):
     assert e.value.status == abi.ERR_INVALID_ARG
     with pytest.raises(abi.TracerError):
         tr.trace_noalloc(fr, p, None, None)
+    # binary traversal only: a 4-wide (or unknown) width is refused
+    for width in (4, 3):
+        wide = abi.Tracer.params(w, h, spp=2, max_depth=4, bvh_width=width)
+        with pytest.raises(abi.TracerError) as e:
+            tr.trace_noalloc(fr, wide, out8.data_ptr(), None)
+        assert e.value.status == abi.ERR_INVALID_ARG

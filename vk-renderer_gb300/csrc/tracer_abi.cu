@@ -156,6 +156,7 @@ struct tracer_ctx {
     tracer_trace_params acc_params;
     uint64_t acc_version = 0;
     DevBuf<unsigned char> pres_src[2], pres_out;  // staging for host images
+    uint32_t trav_cap = 0;            // tracer_set_traversal_limit: 0 = automatic
 };
 
 namespace {
@@ -414,6 +415,14 @@ int pick_width_for(tracer_ctx* c, const tracer_trace_params* p, bool have_wide, 
     return TRACER_OK;
 }
 
+// Traversal steps a ray may take over a BVH of `nodes` nodes: each node is
+// entered at most once per pass, so twice the node count (plus slack) is
+// never reached by a valid BVH; tracer_set_traversal_limit overrides it.
+uint32_t trav_limit(const tracer_ctx* c, uint32_t nodes)
+{
+    return c->trav_cap ? c->trav_cap : 2 * nodes + 16;
+}
+
 int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int& wide)
 {
     const SceneBuffers& s = c->scene;
@@ -545,6 +554,15 @@ void tracer_destroy(tracer_ctx* c)
 }
 
 const char* tracer_last_error(const tracer_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int tracer_set_traversal_limit(tracer_ctx* c, uint32_t steps)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    int r = finish(c);
+    if (r != TRACER_OK) return r;
+    c->trav_cap = steps;
+    return TRACER_OK;
+}
 
 int tracer_set_timeout(tracer_ctx* c, uint32_t ms)
 {
@@ -750,7 +768,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     a.sky_on = !(p->sky[0] == 0.0f && p->sky[1] == 0.0f && p->sky[2] == 0.0f);
     a.stack_depth = stack;
     const uint32_t nn = s.n_tri_nodes > s.n_sph_nodes ? s.n_tri_nodes : s.n_sph_nodes;
-    a.trav_limit = 2 * nn + 16;
+    a.trav_limit = trav_limit(c, nn);
     a.rgba8 = (mask & (1u << TRACER_AOV_RGBA8)) ? c->rgba8.p : nullptr;
     a.rgba32f = (mask & (1u << TRACER_AOV_RGBA32F)) ? c->rgba32f.p : nullptr;
     a.hit = (mask & (1u << TRACER_AOV_PRIMARY_HIT)) ? c->hit.p : nullptr;
@@ -1020,6 +1038,9 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
     if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
         return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
+    if (p->bvh_width != 0 && p->bvh_width != 2)
+        return fail(c, TRACER_ERR_INVALID_ARG, "bvh_width %u: the no-alloc trace runs the binary traversal only (0 or 2)",
+                    p->bvh_width);
     const SceneBuffers& s = c->scene;
     const uint32_t need = s.bvh ? (s.depth > 1 ? s.depth : 1) : 0;
     const uint32_t stack = p->stack_depth ? p->stack_depth : need;
@@ -1052,7 +1073,7 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     a.sky_on = !(p->sky[0] == 0.0f && p->sky[1] == 0.0f && p->sky[2] == 0.0f);
     a.stack_depth = stack;
     const uint32_t nn = s.n_tri_nodes > s.n_sph_nodes ? s.n_tri_nodes : s.n_sph_nodes;
-    a.trav_limit = 2 * nn + 16;
+    a.trav_limit = trav_limit(c, nn);
     a.rgba8 = static_cast<uchar4*>(rgba8_out);
     a.rgba32f = static_cast<float4*>(rgba32f_out);
     a.hit = nullptr;
@@ -1086,13 +1107,14 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     // counters; statistics are not collected here.
     cudaError_t e = cudaMemsetAsync(a.status, 0, sizeof(int), st);
     if (e == cudaSuccess) e = wf_launch_generate(a, ws, wc, st);
-    // No queue length is read back to the host.  Below the hand-over
-    // threshold from the start (always, with the automatic threshold: the
-    // image is smaller than the extend kernel's resident threads), the
+    // No queue length is read back to the host.  With fewer pixels than the
+    // point below which tracer_trace runs no round (tail_paths, or with the
+    // automatic threshold the extend kernel's resident threads -- always the
+    // case here, the image being at most TRACER_NOALLOC_MAX_PIXELS), the
     // finishing kernel traces every pixel in one launch; otherwise every round
     // is launched, and a round with an empty queue returns at once.
-    const uint32_t tail = p->tail_paths ? p->tail_paths : 2 * wc.extend_grid * wc.block;
-    const int fin_per = tail > npx ? wf_finish_blocks_per_sm(wc, stack) : 0;
+    const uint32_t no_rounds_below = p->tail_paths ? p->tail_paths : wc.extend_grid * wc.block;
+    const int fin_per = npx < no_rounds_below ? wf_finish_blocks_per_sm(wc, stack) : 0;
     if (fin_per > 0) {
         const size_t blocks = (npx + 127) / 128, cap = (size_t)fin_per * c->sm_count;
         wc.finish_grid = (uint32_t)(blocks < cap ? blocks : cap);
@@ -1424,7 +1446,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         a.sky = V3{p.sky[0], p.sky[1], p.sky[2]};
         a.sky_on = !(p.sky[0] == 0.0f && p.sky[1] == 0.0f && p.sky[2] == 0.0f);
         a.stack_depth = stack;
-        a.trav_limit = 2 * c->batch_nodes[k] + 16;
+        a.trav_limit = trav_limit(c, c->batch_nodes[k]);
         a.rgba8 = (mask & (1u << TRACER_AOV_RGBA8)) ? c->b_rgba8.p + base[k] : nullptr;
         a.rgba32f = (mask & (1u << TRACER_AOV_RGBA32F)) ? c->b_rgba32f.p + base[k] : nullptr;
         a.hit = (mask & (1u << TRACER_AOV_PRIMARY_HIT)) ? c->b_hit.p + base[k] : nullptr;
@@ -1457,7 +1479,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         TraceArgs a = slots[0];
         a.num_slots = (uint32_t)total;
         a.stack_depth = stack;
-        a.trav_limit = 2 * max_nodes + 16;
+        a.trav_limit = trav_limit(c, max_nodes);
         WfConfig wc;
         std::memset(&wc, 0, sizeof wc);
         wc.tie = TRACER_TIES_STRICT;
@@ -1673,7 +1695,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     a.sky_on = !(p->sky[0] == 0.0f && p->sky[1] == 0.0f && p->sky[2] == 0.0f);
     a.stack_depth = stack;
     const uint32_t nn = s.n_tri_nodes > s.n_sph_nodes ? s.n_tri_nodes : s.n_sph_nodes;
-    a.trav_limit = 2 * nn + 16;
+    a.trav_limit = trav_limit(c, nn);
     a.stats = c->stats.p;
     a.status = c->status.p;
     c->last_rounds = 0;
