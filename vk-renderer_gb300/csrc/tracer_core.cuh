@@ -98,7 +98,8 @@ struct Tracer {
     __device__ __forceinline__ bool traverse(const float4* nodes, uint32_t n_nodes, const Ray& ray, const BoxRay& br,
                                              Hit& h, float tmax, bool any)
     {
-        const float4 rlo = __ldg(nodes), rhi = __ldg(nodes + 1);
+        float4 rlo, rhi;
+        ldg256(nodes, rlo, rhi);
         count(C_NODES);
         float tn;
         if (!box_hit(br, rlo, rhi, h.t, tn)) return false;
@@ -120,7 +121,9 @@ struct Tracer {
                 return false;
             }
             const float4* c = nodes + 2 * (size_t)ci;
-            const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
+            float4 lo0, hi0, lo1, hi1;
+            ldg256(c, lo0, hi0);
+            ldg256(c + 2, lo1, hi1);
             count(C_NODES, 2);
             float t0, t1;
             const bool h0 = box_hit(br, lo0, hi0, h.t, t0);

@@ -146,6 +146,25 @@ __device__ __forceinline__ void psincos(float x, float& s_out, float& c_out)
     s_out = q == 0 ? s : (q == 1 ? c : (q == 2 ? -s : -c));
 }
 
+// ----------------------------------------------------------- 256-bit loads --
+// One 32-byte record through the read-only path as a single 256-bit load
+// (ld.global.nc.v8, sm_100 and later): a BVH node record (box min,
+// reference) (box max, count), or two halves of a wider record.  p must be
+// 32-byte aligned (every device array here starts on a 256-byte boundary and
+// the records are 32 bytes or multiples of it).
+__device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+__device__ __forceinline__ void ldg256u(const void* p, uint32_t (&w)[8])
+{
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+        : "l"(p));
+}
+
 // ------------------------------------------------------------------ RNG --
 // Tracer.comp:221-234: rand() = fract(cos(dot((coords + ++rand_salt) * 5, K1)) * 12345.6789)
 struct Rng {

@@ -140,7 +140,8 @@ __device__ __forceinline__ bool closest_enc(const DevScene& sc, const Ray& ray, 
             L.nodes = pass == 0 ? sc.tri_enc : sc.sph_enc;
             L.sp = 0;
             uint32_t steps = 0;
-            const float4 rlo = __ldg(L.nodes), rhi = __ldg(L.nodes + 1);
+            float4 rlo, rhi;
+            ldg256(L.nodes, rlo, rhi);
             if (STATS) cnt.c[C_NODES]++;
             float tn;
             int cur = box_hit(L.br, rlo, rhi, L.h.t, tn) ? __float_as_int(rlo.w) : 0;
@@ -157,7 +158,9 @@ __device__ __forceinline__ bool closest_enc(const DevScene& sc, const Ray& ray, 
                     break;
                 }
                 const float4* c = L.nodes + 2 * (size_t)cur;
-                const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
+                float4 lo0, hi0, lo1, hi1;
+                ldg256(c, lo0, hi0);
+                ldg256(c + 2, lo1, hi1);
                 if (STATS) cnt.c[C_NODES] += 2;
                 float t0, t1;
                 const bool h0 = box_hit(L.br, lo0, hi0, L.h.t, t0);

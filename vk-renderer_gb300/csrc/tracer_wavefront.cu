@@ -168,7 +168,8 @@ __device__ __forceinline__ void start_pass(const DevScene& sc, Lane& L, Counters
         visit_wide<STATS>(L, 0, stk, status, cnt);
     } else {
         L.nodes = L.pass == 0 ? sc.tri_enc : sc.sph_enc;  // references pre-encoded in bmin.w
-        const float4 lo = __ldg(L.nodes), hi = __ldg(L.nodes + 1);
+        float4 lo, hi;
+        ldg256(L.nodes, lo, hi);
         if (STATS) cnt.c[C_NODES]++;
         float tn;
         L.cur = box_hit(L.br, lo, hi, L.h.t, tn) ? __float_as_int(lo.w) : 0;  // the root may be a leaf
@@ -293,7 +294,9 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     visit_wide<STATS>(L, L.cur, stk, a.status, cnt);
                 } else {
                     const float4* c = L.nodes + 2 * (size_t)L.cur;
-                    const float4 lo0 = __ldg(c), hi0 = __ldg(c + 1), lo1 = __ldg(c + 2), hi1 = __ldg(c + 3);
+                    float4 lo0, hi0, lo1, hi1;
+                    ldg256(c, lo0, hi0);
+                    ldg256(c + 2, lo1, hi1);
                     if (STATS) cnt.c[C_NODES] += 2;
                     float t0, t1;
                     const bool h0 = box_hit(L.br, lo0, hi0, L.h.t, t0);
