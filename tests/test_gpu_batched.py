@@ -70,6 +70,30 @@ def test_batched_equals_single_scene(gpu_tracer, width):
         assert np.array_equal(_bits(tr.readback_scene(k, abi.AOV_RGBA32F)), _bits(singles[k][0])), ("plain", k)
 
 
+def test_batched_cw8_equals_single_scene(gpu_tracer):
+    """A batch of triangle-only scenes through the compressed 8-wide
+    traversal (each scene's nodes and triangles packed in the arena) equals
+    every scene's single-scene binary trace, graph and non-graph."""
+    tr = gpu_tracer
+    scenes = [soup_scene(60, 700), soup_scene(61, 6000, extent=25.0), soup_scene(62, 1), soup_scene(63, 2500)]
+    sizes = [(24, 20), (80, 64), (9, 7), (64, 48)]
+    frames = [S.frame(S.look_at((1.5 * i, 2.0, 30.0), (0.0, 0.0, 0.0), 40.0), w / h, 0.2 * i)
+              for i, (w, h) in enumerate(sizes)]
+    params = [abi.Tracer.params(w, h, spp=2, max_depth=4 + i, rr_start=2, sky=(1.0, 0.9, 0.8),
+                                aovs=(abi.AOV_RGBA32F, abi.AOV_PRIMARY_HIT), kernel=abi.KERNEL_WAVEFRONT,
+                                bvh_width=2, tail_paths=1)
+              for i, (w, h) in enumerate(sizes)]
+    singles = [_single(tr, sc, fr, p) for sc, fr, p in zip(scenes, frames, params)]
+    for p in params:
+        p.bvh_width = 8
+    tr.upload_scenes(scenes)
+    for use_graph in (False, True):
+        tr.trace_batched(frames, params, use_graph=use_graph)
+        for k in range(len(scenes)):
+            assert np.array_equal(_bits(tr.readback_scene(k, abi.AOV_RGBA32F)), _bits(singles[k][0])), (use_graph, k)
+            assert np.array_equal(tr.readback_scene(k, abi.AOV_PRIMARY_HIT), singles[k][1]), (use_graph, k)
+
+
 def test_batched_against_oracle(gpu_tracer):
     tr = gpu_tracer
     scenes, frames, params = _batch()

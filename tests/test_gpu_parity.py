@@ -83,7 +83,9 @@ def test_kernels_identical(gpu_tracer):
 @pytest.mark.parametrize("prims", ["triangles", "spheres", "mixed"])
 def test_wide_traversal_identical(gpu_tracer, prims):
     """The wavefront's 4-wide traversal (nodes collapsed from the binary BVH,
-    same boxes) gives the binary traversal's and the plain kernel's bits."""
+    same boxes) and, for triangle-only scenes, its compressed 8-wide traversal
+    (quantised boxes containing the binary ones) give the binary traversal's
+    and the plain kernel's bits."""
     ref = S.reference_scene()
     if prims == "spheres":
         sc = sphere_scene(3)
@@ -93,8 +95,10 @@ def test_wide_traversal_identical(gpu_tracer, prims):
             sc.spheres = ref.spheres  # one emitter: next-event shadow rays too
     fr = S.frame(S.look_at((0.0, 3.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.2, 0.4)
     out = {}
-    for name, kernel, width in (("plain", abi.KERNEL_PLAIN, 0), ("binary", abi.KERNEL_WAVEFRONT, 2),
-                                ("wide", abi.KERNEL_WAVEFRONT, 4)):
+    runs = [("plain", abi.KERNEL_PLAIN, 0), ("binary", abi.KERNEL_WAVEFRONT, 2), ("wide", abi.KERNEL_WAVEFRONT, 4)]
+    if prims == "triangles":
+        runs.append(("cw8", abi.KERNEL_WAVEFRONT, 8))
+    for name, kernel, width in runs:
         gpu_tracer.upload_scene(sc)
         p = abi.Tracer.params(72, 60, spp=3, max_depth=5, rr_start=2, sky=(0.9, 0.95, 1.0), kernel=kernel,
                               aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F, abi.AOV_PRIMARY_HIT), stats=True,
@@ -102,7 +106,7 @@ def test_wide_traversal_identical(gpu_tracer, prims):
         gpu_tracer.trace(fr, p)
         out[name] = (gpu_tracer.readback(abi.AOV_RGBA32F), gpu_tracer.readback(abi.AOV_PRIMARY_HIT),
                      gpu_tracer.stats())
-    for name in ("binary", "wide"):
+    for name, _, _ in runs[1:]:
         assert np.array_equal(fbits(out[name][0]), fbits(out["plain"][0])), name
         assert np.array_equal(out[name][1], out["plain"][1]), name
         for k in ("closest_rays", "shadow_rays", "hits"):
@@ -120,6 +124,14 @@ def test_wide_traversal_stack_check(gpu_tracer):
     p.bvh_width = 3
     with pytest.raises(abi.TracerError):
         gpu_tracer.trace(fr, p)
+    # an 8-wide traversal needs a triangle-only scene
+    mixed = soup_scene(6, 400)
+    mixed.spheres = sphere_scene(3).spheres
+    gpu_tracer.upload_scene(mixed)
+    p = abi.Tracer.params(16, 16, spp=1, max_depth=2, kernel=abi.KERNEL_WAVEFRONT, bvh_width=8)
+    with pytest.raises(abi.TracerError) as e:
+        gpu_tracer.trace(fr, p)
+    assert e.value.status == abi.ERR_INVALID_ARG
 
 
 def test_bvh_equals_linear_strict(gpu_tracer):

@@ -25,6 +25,7 @@
 #include "tracer_core.cuh"
 #include "tracer_launch.h"
 #include "tracer_present.h"
+#include "bvh_cw8.h"
 #include "bvh_wide.h"
 
 using namespace vkt;
@@ -46,12 +47,15 @@ struct SceneBuffers {
     DevBuf<float4> tri, mats, sph_geo, sph_rec, planes, tri_nodes, sph_nodes;
     DevBuf<float4> tri_wide, sph_wide;  // the BVHs as 4-wide nodes
     DevBuf<float4> tri_enc, sph_enc;    // the binary BVHs with pre-encoded child references
+    DevBuf<float4> tri_cw8, tri_cw8_prims;  // compressed 8-wide BVH over the triangles, triangles in its order
     DevBuf<uint32_t> sph_id, emit;
     uint32_t nt = 0, nm = 0, ns = 0, np = 0, ne = 0;
     uint32_t n_tri_nodes = 0, n_sph_nodes = 0;
     uint32_t depth = 0;       // deepest BVH
     uint32_t wide_depth = 0;  // deepest 4-wide BVH
     bool wide = false;        // 4-wide nodes present
+    uint32_t cw8_depth = 0;   // levels of the 8-wide BVH
+    bool cw8 = false;         // 8-wide BVH present (triangle-only scenes)
     bool bvh = false;
     bool loaded = false;
     void release()
@@ -60,6 +64,8 @@ struct SceneBuffers {
         sph_wide.release();
         tri_enc.release();
         sph_enc.release();
+        tri_cw8.release();
+        tri_cw8_prims.release();
         tri.release();
         mats.release();
         sph_geo.release();
@@ -386,19 +392,32 @@ int run_wavefront(tracer_ctx* c, const TraceArgs& a, WfConfig& wc, size_t nslots
     return TRACER_OK;
 }
 
-// Traversal width of the wavefront's extend kernel: binary unless 4-wide is
-// asked for (bvh_width = 4).  On the soup workloads (100k-1M triangles) the
-// 4-wide traversal measured 8 % slower: visiting a collapsed node tests all
-// four grandchildren's boxes where the binary traversal first culls with the
-// parent's box, and most rays miss most boxes there.  It pushes up to three
-// children per level, so it needs 3 x (its depth) stack entries.
-// stack: in, the binary traversal's stack; out, the stack of the chosen width.
-int pick_width_for(tracer_ctx* c, const tracer_trace_params* p, bool have_wide, uint32_t wide_depth, uint32_t& stack,
-                   int& wide)
+// Traversal width of the wavefront's extend kernel.  bvh_width 8 (and auto,
+// wherever the scene has it: triangle-only scenes) = the compressed 8-wide
+// BVH, which needs no more stack than the binary traversal (at most one node
+// group per 8-wide level); 2 = binary; 4 = the uncompressed 4-wide collapse,
+// measured 8 % slower than binary on the soup workloads (visiting a collapsed
+// node tests all four grandchildren's boxes where the binary traversal first
+// culls with the parent's box, and most rays miss most boxes there); it
+// pushes up to three children per level, so it needs 3 x (its depth) entries.
+// stack: in, the binary traversal's stack; out, the stack of the chosen width
+// (the shade and finishing kernels' binary traversals share it).
+int pick_width_for(tracer_ctx* c, const tracer_trace_params* p, bool have_wide, uint32_t wide_depth, bool have_cw8,
+                   uint32_t cw8_depth, uint32_t& stack, int& wide)
 {
-    wide = 0;
-    if (p->bvh_width != 0 && p->bvh_width != 2 && p->bvh_width != 4)
-        return fail(c, TRACER_ERR_INVALID_ARG, "bvh_width %u must be 0, 2 or 4", p->bvh_width);
+    wide = WF_WIDTH_2;
+    if (p->bvh_width != 0 && p->bvh_width != 2 && p->bvh_width != 4 && p->bvh_width != 8)
+        return fail(c, TRACER_ERR_INVALID_ARG, "bvh_width %u must be 0, 2, 4 or 8", p->bvh_width);
+    if (p->bvh_width == 8 || (p->bvh_width == 0 && have_cw8)) {
+        if (!have_cw8) return fail(c, TRACER_ERR_INVALID_ARG, "the scene has no 8-wide BVH (triangle-only scenes)");
+        if (stack < cw8_depth) {
+            if (p->stack_depth)
+                return fail(c, TRACER_ERR_STACK_OVERFLOW, "8-wide traversal needs a stack of %u entries", cw8_depth);
+            stack = cw8_depth;
+        }
+        wide = WF_WIDTH_8;
+        return TRACER_OK;
+    }
     if (!have_wide || p->bvh_width != 4) {
         if (p->bvh_width == 4) return fail(c, TRACER_ERR_INVALID_ARG, "the scene has no 4-wide BVH");
         return TRACER_OK;
@@ -411,7 +430,7 @@ int pick_width_for(tracer_ctx* c, const tracer_trace_params* p, bool have_wide, 
         return TRACER_OK;
     }
     stack = ws;
-    wide = 1;
+    wide = WF_WIDTH_4;
     return TRACER_OK;
 }
 
@@ -426,7 +445,29 @@ uint32_t trav_limit(const tracer_ctx* c, uint32_t nodes)
 int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int& wide)
 {
     const SceneBuffers& s = c->scene;
-    return pick_width_for(c, p, s.bvh && s.wide, s.wide_depth, stack, wide);
+    return pick_width_for(c, p, s.bvh && s.wide, s.wide_depth, s.bvh && s.cw8, s.cw8_depth, stack, wide);
+}
+
+// The 8-wide BVH of a triangle BVH and the triangles in its order: 64-byte
+// records (v0, original id) (v1 - v0, leaf-ordered slot) (v2 - v0, 0) (0),
+// from the leaf-ordered triangle records `tri` (3 float4 each, as uploaded).
+// Returns false when the scene gets none (bvh_cw8.h).
+bool make_cw8(const std::vector<tracer_bvh_node>& tnodes, const std::vector<float4>& tri, std::vector<Cw8Node>& nodes,
+              std::vector<float4>& prims, uint32_t& depth)
+{
+    std::vector<uint32_t> order;
+    if (tnodes.empty() || !build_cw8(tnodes.data(), (uint32_t)tnodes.size(), nodes, order, &depth)) return false;
+    prims.assign(4 * order.size(), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (size_t k = 0; k < order.size(); ++k) {
+        const uint32_t slot = order[k];
+        const float4 a = tri[3 * (size_t)slot], b = tri[3 * (size_t)slot + 1], e = tri[3 * (size_t)slot + 2];
+        float fslot;
+        std::memcpy(&fslot, &slot, 4);
+        prims[4 * k + 0] = make_float4(a.x, a.y, a.z, b.w);  // v0, original id
+        prims[4 * k + 1] = make_float4(b.x, b.y, b.z, fslot);
+        prims[4 * k + 2] = make_float4(e.x, e.y, e.z, 0.0f);
+    }
+    return true;
 }
 
 // Builds (or validates) one BVH; returns the leaf-order permutation.
@@ -649,6 +690,10 @@ int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
     if (!encode_refs(tnodes.data(), (uint32_t)tnodes.size(), tenc) ||
         !encode_refs(snodes.data(), (uint32_t)snodes.size(), senc))
         return fail(c, TRACER_ERR_BAD_BVH, "a BVH leaf holds more than 64 primitives or starts beyond 2^25");
+    std::vector<Cw8Node> cw8;
+    std::vector<float4> cw8_prims;
+    uint32_t cw8_depth = 0;
+    const bool cw8_ok = s.bvh && s.nt > 0 && s.ns == 0 && make_cw8(tnodes, tri, cw8, cw8_prims, cw8_depth);
 
     cudaError_t e = upload(s.tri, tri.data(), tri.size());
     if (e == cudaSuccess) e = upload(s.mats, reinterpret_cast<const float4*>(d->materials), 3 * (size_t)s.nm);
@@ -667,11 +712,15 @@ int tracer_upload_scene(tracer_ctx* c, const tracer_scene_desc* d)
         e = upload(s.tri_wide, reinterpret_cast<const float4*>(twide.data()), 8 * twide.size());
     if (e == cudaSuccess && wide_ok)
         e = upload(s.sph_wide, reinterpret_cast<const float4*>(swide.data()), 8 * swide.size());
+    if (e == cudaSuccess && cw8_ok) e = upload(s.tri_cw8, reinterpret_cast<const float4*>(cw8.data()), 6 * cw8.size());
+    if (e == cudaSuccess && cw8_ok) e = upload(s.tri_cw8_prims, cw8_prims.data(), cw8_prims.size());
     if (e != cudaSuccess) {
         s.release();
         return cuda_fail(c, e, "scene upload");
     }
     s.wide = wide_ok;
+    s.cw8 = cw8_ok;
+    s.cw8_depth = cw8_depth;
     s.loaded = true;
     ++c->scene_version;
     return TRACER_OK;
@@ -751,7 +800,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
     const SceneBuffers& s = c->scene;
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p, s.tri_cw8.p, s.tri_cw8_prims.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     const tracer_camera& cam = f->camera;
@@ -1057,7 +1106,7 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p, s.tri_cw8.p, s.tri_cw8_prims.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
@@ -1140,8 +1189,10 @@ struct PackedScene {
     std::vector<uint32_t> sid, emit;
     std::vector<tracer_bvh_node> tnodes, snodes, tenc, senc;
     std::vector<WideNode> twide, swide;
-    uint32_t depth = 0, wide_depth = 0;
-    bool wide = false;
+    std::vector<Cw8Node> cw8;
+    std::vector<float4> cw8_prims;
+    uint32_t depth = 0, wide_depth = 0, cw8_depth = 0;
+    bool wide = false, cw8_ok = false;
     int status = TRACER_OK;
 };
 
@@ -1216,6 +1267,8 @@ void pack_scene(const tracer_scene_desc& d, PackedScene& out)
         const float* em = d.spheres[i].mat.emissive;
         if (!(em[0] == 0.0f && em[1] == 0.0f && em[2] == 0.0f)) out.emit.push_back(i);
     }
+    out.cw8_ok = d.num_triangles > 0 && d.num_spheres == 0 &&
+                 make_cw8(out.tnodes, out.tri, out.cw8, out.cw8_prims, out.cw8_depth);
 }
 
 int validate_desc(tracer_ctx* c, const tracer_scene_desc& d, uint32_t k)
@@ -1263,18 +1316,26 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
             return fail(c, packed[k].status, "scene %u: BVH build or validation failed", k);
 
     // one arena per array kind, scenes back to back
-    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes, twide, swide, tenc, senc;
+    std::vector<float4> tri, mats, geo, rec, planes, tnodes, snodes, twide, swide, tenc, senc, tcw8, tcw8p;
     std::vector<uint32_t> sid, emit;
     struct Off {
-        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit, twide, swide, tenc, senc;
+        size_t tri, mats, geo, rec, planes, tnodes, snodes, sid, emit, twide, swide, tenc, senc, tcw8, tcw8p;
     };
     std::vector<Off> off(n);
-    bool wide_all = true;
+    bool wide_all = true, cw8_all = true;
+    for (uint32_t k = 0; k < n; ++k)
+        cw8_all = cw8_all && packed[k].cw8_ok;
     for (uint32_t k = 0; k < n; ++k) {
         const tracer_scene_desc& d = descs[k];
         const PackedScene& p = packed[k];
-        off[k] = Off{tri.size(), mats.size(), geo.size(), rec.size(), planes.size(), tnodes.size(), snodes.size(),
-                     sid.size(), emit.size(), twide.size(), swide.size(), tenc.size(), senc.size()};
+        off[k] = Off{tri.size(),    mats.size(),  geo.size(),  rec.size(),  planes.size(),
+                     tnodes.size(), snodes.size(), sid.size(), emit.size(), twide.size(),
+                     swide.size(),  tenc.size(),  senc.size(), tcw8.size(), tcw8p.size()};
+        if (cw8_all) {  // 6 and 4 float4 per record: every scene's part stays 32-byte aligned
+            const float4* cn = reinterpret_cast<const float4*>(p.cw8.data());
+            tcw8.insert(tcw8.end(), cn, cn + 6 * p.cw8.size());
+            tcw8p.insert(tcw8p.end(), p.cw8_prims.begin(), p.cw8_prims.end());
+        }
         const float4* te = reinterpret_cast<const float4*>(p.tenc.data());
         tenc.insert(tenc.end(), te, te + 2 * p.tenc.size());
         const float4* se = reinterpret_cast<const float4*>(p.senc.data());
@@ -1314,12 +1375,16 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
     if (e == cudaSuccess) e = upload(b.sph_enc, senc.data(), senc.size());
     if (e == cudaSuccess && wide_all) e = upload(b.tri_wide, twide.data(), twide.size());
     if (e == cudaSuccess && wide_all) e = upload(b.sph_wide, swide.data(), swide.size());
+    if (e == cudaSuccess && cw8_all) e = upload(b.tri_cw8, tcw8.data(), tcw8.size());
+    if (e == cudaSuccess && cw8_all) e = upload(b.tri_cw8_prims, tcw8p.data(), tcw8p.size());
     if (e != cudaSuccess) {
         b.release();
         return cuda_fail(c, e, "batch upload");
     }
     b.wide = wide_all;
     b.wide_depth = 0;
+    b.cw8 = cw8_all;
+    b.cw8_depth = 0;
     c->batch_scenes.assign(n, DevScene{});
     c->batch_depth.assign(n, 0);
     c->batch_nodes.assign(n, 0);
@@ -1336,8 +1401,11 @@ extern "C" int tracer_upload_scenes(tracer_ctx* c, const tracer_scene_desc* desc
                                       (uint32_t)p.snodes.size(),
                                       wide_all ? at(b.tri_wide, off[k].twide) : nullptr,
                                       wide_all ? at(b.sph_wide, off[k].swide) : nullptr,
-                                      at(b.tri_enc, off[k].tenc), at(b.sph_enc, off[k].senc)};
+                                      at(b.tri_enc, off[k].tenc), at(b.sph_enc, off[k].senc),
+                                      cw8_all ? at(b.tri_cw8, off[k].tcw8) : nullptr,
+                                      cw8_all ? at(b.tri_cw8_prims, off[k].tcw8p) : nullptr};
         b.wide_depth = std::max(b.wide_depth, p.wide_depth);
+        b.cw8_depth = std::max(b.cw8_depth, p.cw8_depth);
         c->batch_depth[k] = p.depth;
         c->batch_nodes[k] = (uint32_t)std::max(p.tnodes.size(), p.snodes.size());
         c->batch_emitters = c->batch_emitters || !p.emit.empty();
@@ -1377,7 +1445,8 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         return fail(c, TRACER_ERR_INVALID_ARG, "stack depth %u exceeds shared memory", stack);
     int wide = 0;
     if (kernel == TRACER_KERNEL_WAVEFRONT) {
-        int rw = pick_width_for(c, &p0, c->batch.wide, c->batch.wide_depth, stack, wide);
+        int rw = pick_width_for(c, &p0, c->batch.wide, c->batch.wide_depth, c->batch.cw8, c->batch.cw8_depth, stack,
+                                wide);
         if (rw != TRACER_OK) return rw;
     }
     const uint32_t mask = p0.aov_mask ? p0.aov_mask : (1u << TRACER_AOV_RGBA8);
@@ -1679,7 +1748,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p, s.tri_cw8.p, s.tri_cw8_prims.p};
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};

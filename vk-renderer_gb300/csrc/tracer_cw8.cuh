@@ -1,0 +1,132 @@
+// Device side of the compressed 8-wide BVH (layout: bvh_cw8.h): one node's
+// eight quantised slab tests and the node groups a traversal keeps.
+//
+// A node group is (child_base, remaining hit interior children << 24 | imask):
+// bit 24 + (k ^ s ^ 7) stands for slot k (s = the ray's direction octant), so
+// the highest set bit is the next child to visit and slot k's node index is
+// child_base + popc(imask & ((1 << k) - 1)).  A primitive group is
+// (prim_base, bit i = primitive prim_base + i still to test).
+#pragma once
+
+#include "tracer_traverse.cuh"
+
+namespace vkt {
+
+// The ray's quantities for the 8-wide slab test: the direction octant and,
+// per axis, the slab planes' order (near plane = low bound for a
+// non-negative inverse direction).
+struct Cw8Ray {
+    BoxRay br;
+    uint32_t oct7;  // (octant s) ^ 7
+};
+
+__device__ __forceinline__ Cw8Ray make_cw8ray(const Ray& r)
+{
+    Cw8Ray c;
+    c.br = make_boxray(r);
+    const uint32_t s = (c.br.ix < 0.0f ? 1u : 0u) | (c.br.iy < 0.0f ? 2u : 0u) | (c.br.iz < 0.0f ? 4u : 0u);
+    c.oct7 = s ^ 7u;
+    return c;
+}
+
+__device__ __forceinline__ float ubyte_f(uint32_t w, int k)
+{
+    return __uint2float_rn((w >> (8 * k)) & 0xFFu);
+}
+
+// Visits node `idx`: tests its children's boxes against the ray with the
+// current best distance tbest and returns the node group of the interior
+// children hit (G) and the primitive group of the leaf children hit (P).
+// Each box is [p + q_lo * step, p + q_hi * step] per axis, which contains
+// the binary child's padded box; the slab distances are
+// fma(q, step * ix, fma(p, ix, -o * ix)), and a child is hit iff
+// max(near distances, 0) <= min(far distances, tbest) * (1 + 2^-20): the
+// binary test's acceptance, on a box that contains the binary box, so every
+// box the binary traversal enters is entered here too.
+__device__ __forceinline__ void cw8_visit(const float4* nodes, uint32_t idx, const Cw8Ray& r, float tbest, uint2& G,
+                                          uint2& P)
+{
+    uint32_t a[8], b[8], c[8];
+    const float4* n = nodes + 6 * (size_t)idx;
+    ldg256u(n, a);
+    ldg256u(n + 2, b);
+    ldg256u(n + 4, c);
+    const float px = __uint_as_float(a[0]), py = __uint_as_float(a[1]), pz = __uint_as_float(a[2]);
+    const float sx = __uint_as_float((a[3] & 0xFFu) << 23);
+    const float sy = __uint_as_float(((a[3] >> 8) & 0xFFu) << 23);
+    const float sz = __uint_as_float(((a[3] >> 16) & 0xFFu) << 23);
+    const float ax = sx * r.br.ix, ay = sy * r.br.iy, az = sz * r.br.iz;
+    const float bx = __fmaf_rn(px, r.br.ix, r.br.nx);
+    const float by = __fmaf_rn(py, r.br.iy, r.br.ny);
+    const float bz = __fmaf_rn(pz, r.br.iz, r.br.nz);
+    // near / far plane words per axis (two words = eight slots)
+    const bool fx = r.br.ix < 0.0f, fy = r.br.iy < 0.0f, fz = r.br.iz < 0.0f;
+    // b = w8..w15: lo x (b0, b1), lo y (b2, b3), lo z (b4, b5), hi x (b6, b7)
+    // c = w16..w23: hi y (c0, c1), hi z (c2, c3)
+    const uint32_t lox[2] = {b[0], b[1]}, loy[2] = {b[2], b[3]}, loz[2] = {b[4], b[5]};
+    const uint32_t hix[2] = {b[6], b[7]}, hiy[2] = {c[0], c[1]}, hiz[2] = {c[2], c[3]};
+    uint32_t hits = 0, prims = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t qnx = fx ? hix[h] : lox[h], qfx = fx ? lox[h] : hix[h];
+        const uint32_t qny = fy ? hiy[h] : loy[h], qfy = fy ? loy[h] : hiy[h];
+        const uint32_t qnz = fz ? hiz[h] : loz[h], qfz = fz ? loz[h] : hiz[h];
+        const uint32_t meta = a[6 + h];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float tnx = __fmaf_rn(ubyte_f(qnx, k), ax, bx);
+            const float tny = __fmaf_rn(ubyte_f(qny, k), ay, by);
+            const float tnz = __fmaf_rn(ubyte_f(qnz, k), az, bz);
+            const float tfx = __fmaf_rn(ubyte_f(qfx, k), ax, bx);
+            const float tfy = __fmaf_rn(ubyte_f(qfy, k), ay, by);
+            const float tfz = __fmaf_rn(ubyte_f(qfz, k), az, bz);
+            const float tmin = fmaxf(fmax3(tnx, tny, tnz), 0.0f);
+            const float tmax = fminf(fmin3(tfx, tfy, tfz), tbest);
+            const uint32_t m = (meta >> (8 * k)) & 0xFFu;
+            if (tmin <= tmax * BOX_SLACK) {
+                const uint32_t cnt = m >> 5;
+                const int slot = 4 * h + k;
+                if (cnt == 7u)
+                    hits |= 1u << (24 + (slot ^ r.oct7));
+                else
+                    prims |= ((1u << cnt) - 1u) << (m & 31u);
+            }
+        }
+    }
+    G = make_uint2(a[4], hits | (a[3] >> 24));
+    P = make_uint2(a[5], prims);
+}
+
+// Takes the next child of a node group (which has one): its node index; the
+// group keeps the others.
+__device__ __forceinline__ uint32_t cw8_next(uint2& G, uint32_t oct7)
+{
+    const int bit = 31 - __clz(G.y);
+    const uint32_t slot = (uint32_t)(bit - 24) ^ oct7;
+    G.y &= ~(1u << bit);
+    return G.x + __popc(G.y & ((1u << slot) - 1u) & 0xFFu);
+}
+
+// Tests primitive k of the 8-wide order: a 64-byte record
+// (v0, original id) (v1 - v0, leaf-ordered slot) (v2 - v0, 0) (0), read as two
+// 256-bit loads; on acceptance the hit records the leaf-ordered slot (the
+// storage slot every other kernel indexes).
+template <bool STATS>
+__device__ __forceinline__ void cw8_test_tri(const float4* tris, uint32_t k, const Ray& ray, Hit& h, Counters& cnt)
+{
+    if (STATS) cnt.c[C_TRIS]++;
+    float4 ta, tb, tc, td;
+    ldg256(tris + 4 * (size_t)k, ta, tb);
+    ldg256(tris + 4 * (size_t)k + 2, tc, td);
+    (void)td;
+    const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
+    const uint32_t id = __float_as_uint(ta.w);
+    if (accept_strict(tt, id, h)) {
+        h.t = tt;
+        h.prim = id;
+        h.kind = 1;
+        h.slot = __float_as_uint(tb.w);
+    }
+}
+
+}  // namespace vkt

@@ -219,6 +219,8 @@ struct DevScene {
     const float4* sph_wide;
     const float4* tri_enc;   // the binary nodes with each record's child reference pre-encoded in
     const float4* sph_enc;   // bmin's w lane (interior: children-pair index; leaf: leaf code)
+    const float4* tri_cw8;        // compressed 8-wide nodes over the triangles (6 float4 each), or NULL
+    const float4* tri_cw8_prims;  // the triangles in their 8-wide order, 64 B each
 };
 
 struct Counters {

@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 
 #include "tracer_core.cuh"
+#include "tracer_cw8.cuh"
 #include "tracer_traverse.cuh"
 #include "tracer_wavefront.h"
 
@@ -350,6 +351,157 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     if (STATS) flush_counters(a, cnt);
 }
 
+// Primitive groups a lane of the 8-wide traversal may hold back while the
+// warp's slowest lane is still looking for its first.
+constexpr int kCw8Postpone = 2;
+
+// The extend kernel over the compressed 8-wide BVH (triangle scenes; strict
+// ties).  Same phases as wf_extend_bvh: idle lanes fetch rays; all lanes visit
+// 8-wide nodes (one per lane and step: eight quantised slab tests, the hit
+// interior children become a node group on the stack, the hit leaves a
+// primitive group held back) until every lane still tracing holds some
+// primitives, lanes that hold fewer than kCw8Postpone groups going on; then
+// all lanes test their held primitives, one per lane and step.  Node groups
+// are visited nearest-octant first; which boxes are entered depends on the
+// order, the closest hit under strict ties does not.
+template <bool STATS, bool MULTI, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
+    wf_extend_cw8(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
+{
+    extern __shared__ int smem[];
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    // stack of node groups, then held primitive groups; entry j of a thread
+    // at j * BLOCK + threadIdx.x
+    uint2* stk = reinterpret_cast<uint2*>(smem) + threadIdx.x;
+    uint2* held = reinterpret_cast<uint2*>(smem) + (size_t)a.stack_depth * BLOCK + threadIdx.x;
+    const int cap = (int)a.stack_depth;
+    const uint32_t total = s.count[qsel];
+    const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.count[qsel ^ 1] = 0;
+    Counters cnt;
+#pragma unroll
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    bool has = false, exhausted = false;
+    uint32_t pid = 0, scene = 0, steps = 0;
+    Ray ray{};
+    Cw8Ray cr{};
+    Hit h{};
+    uint2 G = make_uint2(0u, 0u);
+    int sp = 0, nh = 0;
+    const float4* nodes = nullptr;
+    const float4* tris = nullptr;
+    for (;;) {
+        // 1) idle lanes take the next rays of the queue
+        const unsigned need = __ballot_sync(full, !has && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&s.count[2], (uint32_t)__popc(need));
+            base = __shfl_sync(full, base, leader);
+            if (!has && !exhausted) {
+                const uint32_t qi = base + __popc(need & ((1u << lane) - 1u));
+                if (qi >= total) {
+                    exhausted = true;
+                } else {
+                    pid = queue[qi];
+                    scene = MULTI ? s.scene_of[pid] : 0;
+                    const DevScene& sc = SCENE_ARGS(MULTI, a, slots, scene).sc;
+                    const float4 ro = s.ray_o[pid];
+                    const float4 rd = s.ray_d[pid];
+                    ray = Ray{v3(ro), v3(rd)};
+                    h.t = ro.w;
+                    h.prim = 0;  // see accept_strict
+                    h.kind = 0;
+                    h.slot = 0;
+                    steps = 0;
+                    if (STATS) cnt.c[C_CLOSEST]++;
+                    has = true;
+                    if (isnan3(ray.d) || !(sc.n_tri_nodes > 0 && sc.nt > 0)) {
+                        // no BVH work: NaN directions hit nothing; planes only
+                        if (!isnan3(ray.d)) planes_pass<STATS>(sc, ray, h, cnt);
+                        if (STATS && h.kind) cnt.c[C_HITS]++;
+                        s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+                        has = false;
+                    } else {
+                        cr = make_cw8ray(ray);
+                        nodes = sc.tri_cw8;
+                        tris = sc.tri_cw8_prims;
+                        // the root: the one interior child (slot 0) of a group of its own
+                        G = make_uint2(0u, (1u << (24 + (0u ^ cr.oct7))) | 1u);
+                        sp = 0;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(full, has)) {
+            if (__all_sync(full, exhausted)) break;
+            continue;
+        }
+        // 2) nodes, until every lane still tracing holds primitives
+        for (;;) {
+            const bool search = has && nh < kCw8Postpone && ((G.y & 0xFF000000u) != 0u || sp > 0);
+            if (!__any_sync(full, search && nh == 0)) break;
+            if (search) {
+                if ((G.y & 0xFF000000u) == 0u) {
+                    --sp;
+                    G = stk[sp * BLOCK];
+                }
+                if (++steps > a.trav_limit) {
+                    atomicCAS(a.status, ST_OK, ST_TRAVERSAL_LIMIT);
+                    G = make_uint2(0u, 0u);
+                    sp = 0;
+                } else {
+                    const uint32_t idx = cw8_next(G, cr.oct7);
+                    if (G.y & 0xFF000000u) {
+                        if (sp >= cap) {
+                            atomicCAS(a.status, ST_OK, ST_STACK_OVERFLOW);
+                        } else {
+                            stk[sp * BLOCK] = G;
+                            ++sp;
+                        }
+                    }
+                    uint2 P;
+                    cw8_visit(nodes, idx, cr, h.t, G, P);
+                    if (STATS) cnt.c[C_NODES] += 3;
+                    if (P.y) {
+                        held[nh * BLOCK] = P;
+                        ++nh;
+                    }
+                }
+            }
+        }
+        // 3) the held primitives, one per lane and step
+        {
+            int j = 0;
+            uint2 cur = make_uint2(0u, 0u);
+            for (;;) {
+                const bool lf = has && (cur.y != 0u || j < nh);
+                if (!__any_sync(full, lf)) break;
+                if (lf) {
+                    if (cur.y == 0u) {
+                        cur = held[j * BLOCK];
+                        ++j;
+                    }
+                    const int bit = __ffs(cur.y) - 1;
+                    cur.y &= cur.y - 1u;
+                    cw8_test_tri<STATS>(tris, cur.x + (uint32_t)bit, ray, h, cnt);
+                }
+            }
+        }
+        nh = 0;
+        // 4) finished rays: planes and the result
+        if (has && (G.y & 0xFF000000u) == 0u && sp == 0) {
+            const DevScene& sc = SCENE_ARGS(MULTI, a, slots, scene).sc;
+            planes_pass<STATS>(sc, ray, h, cnt);
+            if (STATS && h.kind) cnt.c[C_HITS]++;
+            s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+            has = false;
+        }
+    }
+    if (STATS) flush_counters(a, cnt);
+}
+
 // Linear-scan scenes (the reference's own trace_ray, reference or strict ties):
 // persistent lanes with a per-warp fetch.  Single scene only.
 template <int TIE, bool STATS>
@@ -555,17 +707,20 @@ static void smem_attr(K k, size_t smem)
 }
 
 // Dynamic shared memory of the extend kernel: every thread's traversal stack
-// (8 B per entry) and postponed-leaf buffer (4 B per entry).
-static size_t wf_extend_smem(size_t stack_depth, uint32_t block)
+// (8 B per entry) and its held leaves (binary and 4-wide: 4 B per leaf
+// reference) or held primitive groups (8-wide: 8 B per group).
+static size_t wf_extend_smem(size_t stack_depth, uint32_t block, int wide)
 {
-    return (stack_depth * 8 + kPostpone * 4) * block;
+    return (stack_depth * 8 + (wide == WF_WIDTH_8 ? kCw8Postpone * 8 : kPostpone * 4)) * block;
 }
 
 template <int TIE, bool STATS, bool MULTI, int BLOCK>
 static cudaError_t extend_bvh_b(const TraceArgs& a, const WfState& s, const WfConfig& c, int qsel, cudaStream_t st)
 {
-    auto k = c.wide ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true> : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
-    const size_t smem = wf_extend_smem(a.stack_depth, BLOCK);
+    auto k = c.wide == WF_WIDTH_8   ? wf_extend_cw8<STATS, MULTI, BLOCK>
+             : c.wide == WF_WIDTH_4 ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true>
+                                    : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
+    const size_t smem = wf_extend_smem(a.stack_depth, BLOCK, c.wide);
     smem_attr(k, smem);
     k<<<c.extend_grid, BLOCK, smem, st>>>(a, s, qsel, c.slots);
     return cudaGetLastError();
@@ -674,18 +829,20 @@ int wf_finish_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
 }
 
 template <int TIE, bool STATS, bool MULTI, int BLOCK>
-static cudaError_t occ_bvh_b(int& n, bool wide, size_t smem)
+static cudaError_t occ_bvh_b(int& n, int wide, size_t smem)
 {
-    auto k = wide ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true> : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
+    auto k = wide == WF_WIDTH_8   ? wf_extend_cw8<STATS, MULTI, BLOCK>
+             : wide == WF_WIDTH_4 ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true>
+                                  : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
     smem_attr(k, smem);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, BLOCK, smem);
 }
 
 template <int TIE, bool STATS, bool MULTI>
-static int occ_bvh(uint32_t block, size_t stack_depth, bool wide)
+static int occ_bvh(uint32_t block, size_t stack_depth, int wide)
 {
     int n = 0;
-    const size_t smem = wf_extend_smem(stack_depth, block);
+    const size_t smem = wf_extend_smem(stack_depth, block, wide);
     cudaError_t e;
     if (block == 64)
         e = occ_bvh_b<TIE, STATS, MULTI, 64>(n, wide, smem);
@@ -698,7 +855,7 @@ static int occ_bvh(uint32_t block, size_t stack_depth, bool wide)
 
 int wf_extend_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
 {
-    const bool w = c.wide != 0;
+    const int w = c.wide;
     if (c.multi) return c.stats ? occ_bvh<TIE_STRICT, true, true>(c.block, stack_depth, w)
                                 : occ_bvh<TIE_STRICT, false, true>(c.block, stack_depth, w);
     if (c.bvh) return c.stats ? occ_bvh<TIE_STRICT, true, false>(c.block, stack_depth, w)

@@ -8,6 +8,10 @@ namespace vkt {
 
 struct TraceArgs;
 
+// BVH the extend kernel traverses: the binary BVH, its 4-wide collapse, or
+// its compressed 8-wide collapse (bvh_wide.h, bvh_cw8.h).
+enum : int { WF_WIDTH_2 = 0, WF_WIDTH_4 = 1, WF_WIDTH_8 = 2 };
+
 // One slot per pixel (index = scene's pixel_base + y * width + x), structure
 // of arrays.
 struct WfState {
@@ -27,7 +31,7 @@ struct WfConfig {
     int tie, bvh, stats;
     int multi;                // batched: per-slot scene table
     int has_emitters;         // some scene has emissive spheres (shade needs a traversal stack)
-    int wide;                 // extend traverses the 4-wide nodes (every scene has them)
+    int wide;                 // extend's BVH: WF_WIDTH_2 (binary), WF_WIDTH_4 or WF_WIDTH_8 (every scene has it)
     uint32_t block;           // extend kernel threads per block: 64, 128 or 256
     uint32_t extend_grid, shade_grid;
     uint32_t finish_grid;     // blocks of 128 threads of the finishing kernel
