@@ -140,18 +140,26 @@ int main(int argc, char** argv)
         const uint32_t* x = w[i].w;
         const uint32_t imask = x[3] >> 24;
         int ni = 0;
+        uint32_t used = 0;
         for (int k = 0; k < 8; ++k) {
-            const uint32_t m = byte_of(x[6 + k / 4], k % 4), c = m >> 5;
-            if (((imask >> k) & 1u) != (c == 7u ? 1u : 0u)) fail("imask", (long)i, k);
-            if (c == 7u) ++ni;
-            if (c >= 1 && c <= 6 && (m & 31u) + c > 24u) fail("leaf bits", (long)i, k);
-            if (c == 0 && m != 0) fail("empty meta", (long)i, k);
+            const uint32_t xm = byte_of(x[6 + k / 4], k % 4), bits = byte_of(x[20 + k / 4], k % 4),
+                           pos = byte_of(x[22 + k / 4], k % 4);
+            const bool inner = (imask >> k) & 1u;
+            if (xm != (inner ? 7u : 0u)) fail("octant mask", (long)i, k);
+            if (inner) {
+                ++ni;
+                if (bits != 1u || pos != 24u + (uint32_t)k) fail("interior bits", (long)i, k);
+            } else if (bits != 0u) {
+                const uint32_t c = (uint32_t)__builtin_popcount(bits);
+                if (bits != (1u << c) - 1u || c > vkt::kCw8MaxLeafPrims || pos + c > 24u) fail("leaf bits", (long)i, k);
+                if (used & (bits << pos)) fail("overlapping leaves", (long)i, k);
+                used |= bits << pos;
+                if ((size_t)x[5] + pos + c > n) fail("prim range", (long)i, k);
+            } else if (pos != 0u) {
+                fail("empty slot", (long)i, k);
+            }
         }
         if (ni && (size_t)x[4] + ni > w.size()) fail("child range", (long)i, x[4]);
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t m = byte_of(x[6 + k / 4], k % 4), c = m >> 5;
-            if (c >= 1 && c <= 6 && (size_t)x[5] + (m & 31u) + c > n) fail("prim range", (long)i, k);
-        }
     }
     // traversal emulation against a brute-force scan
     std::vector<float> v0(3 * (size_t)n), e1(3 * (size_t)n), e2(3 * (size_t)n);
@@ -200,7 +208,7 @@ int main(int argc, char** argv)
             const float ax = sx * ix, ay = sy * iy, az = sz * iz;
             const float bx = std::fma(f_of(x[0]), ix, nx), by = std::fma(f_of(x[1]), iy, ny),
                         bz = std::fma(f_of(x[2]), iz, nz);
-            uint32_t hitsm = 0, prims = 0;
+            uint32_t mask = 0;
             for (int k = 0; k < 8; ++k) {
                 const int h = k / 4, kk = k % 4;
                 const float lx = (float)byte_of(x[8 + h], kk), ly = (float)byte_of(x[10 + h], kk),
@@ -211,19 +219,14 @@ int main(int argc, char** argv)
                 const float tnz = std::fma(iz < 0 ? hz : lz, az, bz), tfz = std::fma(iz < 0 ? lz : hz, az, bz);
                 const float tmn = std::fmax(std::fmax(std::fmax(tnx, tny), tnz), 0.0f);
                 const float tmx = std::fmin(std::fmin(std::fmin(tfx, tfy), tfz), b.t);
-                const uint32_t m = byte_of(x[6 + h], kk), c = m >> 5;
-                if (tmn <= tmx * (1.0f + 0x1.0p-20f)) {
-                    if (c == 7u)
-                        hitsm |= 1u << (24 + (k ^ oct7));
-                    else
-                        prims |= ((1u << c) - 1u) << (m & 31u);
-                }
+                const uint32_t bits = byte_of(x[20 + h], kk), pos = byte_of(x[22 + h], kk) ^ (oct7 & byte_of(x[6 + h], kk));
+                if (tmn <= tmx * (1.0f + 0x1.0p-20f)) mask |= bits << pos;
             }
-            for (uint32_t p = prims; p; p &= p - 1) {
+            for (uint32_t p = mask & 0x00FFFFFFu; p; p &= p - 1) {
                 const uint32_t k = x[5] + __builtin_ctz(p);
                 accept(b, tri_t(o, d, &v0[3 * k], &e1[3 * k], &e2[3 * k]), orig[k]);
             }
-            G = (uint64_t)(hitsm | (x[3] >> 24)) << 32 | x[4];
+            G = (uint64_t)((mask & 0xFF000000u) | (x[3] >> 24)) << 32 | x[4];
         }
         if (b.t != brute.t || b.id != brute.id) fail("closest hit differs", r, (long)b.id);
         if (brute.t < tmax) ++hits;

@@ -152,7 +152,9 @@ def test_timings_after_graph_and_autotune(gpu_tracer):
                                         tails=(0, 1))
     assert best is not None and best["ms"] > 0
     assert any("skipped" in r for r in table)  # stack 4 is below the BVH depth
-    assert len(table) == 32  # widths 4 and 2, tails auto and never
+    assert len(table) == 48  # widths 8, 4 and 2, tails auto and never
+    # the batch has spheres: no 8-wide BVH, those candidates are refused
+    assert all("skipped" in r for r in table if r["bvh_width"] == 8)
     assert best["bvh_width"] in (2, 4) and best["tail_paths"] in (0, 1)
     assert all(p.tail_paths == 0 for p in params)  # the parameters are restored
 

@@ -63,11 +63,34 @@ def test_autotune_picks_fastest_and_restores_params():
     skipped = [r for r in table if "skipped" in r]
     assert skipped and all(r["stack_depth"] == 4 for r in skipped)
     assert all("stack depth" in r["skipped"] for r in skipped)
-    # every candidate traced once to capture and reps times to time (refused ones once)
-    assert len(tr.calls) == (len(table) - len(skipped)) * 3 + len(skipped)
+    # every candidate traced once to capture and reps times to time (refused ones once), then
+    # the 3 fastest once more to capture and 5 times each
+    assert len(tr.calls) == (len(table) - len(skipped)) * 3 + len(skipped) + 3 * (1 + 5)
+    refined = [r for r in table if "ms_refined" in r]
+    assert len(refined) == 3 and min(r["ms_refined"] for r in refined) == best["ms"]
     for p in params:
         assert (p.block, p.stack_depth, p.wavefront, p.bvh_width, p.tail_paths) == (0, 0, 0, 0, 0)
     assert not tr.profiling
+
+
+def test_autotune_refine_overrules_a_noisy_first_sample():
+    """A candidate that was lucky once loses to the one whose repeated
+    timings are faster."""
+    tr = FakeTracer()
+    lucky = {"n": 0}
+    base_trace = tr.trace_batched
+
+    def trace(frames, params, use_graph=True):
+        base_trace(frames, params, use_graph)
+        p = params[0]
+        if p.block == 256:  # a slow shape with one lucky sample in the sweep
+            lucky["n"] += 1
+            tr.last_ms = 5.0 if lucky["n"] == 2 else 30.0
+    tr.trace_batched = trace
+    best, table = tune.autotune_batched(tr, [None], _params(1), blocks=(128, 256), stacks=(0,), wavefronts=(6,),
+                                        widths=(2,), tails=(1000,), reps=1)
+    assert [r["ms"] for r in table if r["block"] == 256] == [5.0]
+    assert best["block"] == 128 and best["ms"] == pytest.approx(10.0)
 
 
 def test_autotune_time_budget():

@@ -178,10 +178,13 @@ bool build_cw8(const tracer_bvh_node* nodes, uint32_t num_nodes, std::vector<Cw8
             }
             if (is_leaf(n)) {
                 const uint32_t o = (uint32_t)order_out.size() - prim_base;
-                put_byte(node.w + 6, s, (uint32_t)n.count << 5 | o);
+                put_byte(node.w + 20, s, (1u << n.count) - 1u);
+                put_byte(node.w + 22, s, o);
                 for (int32_t j = 0; j < n.count; ++j) order_out.push_back((uint32_t)(n.left_or_first + j));
             } else {
-                put_byte(node.w + 6, s, 7u << 5);
+                put_byte(node.w + 6, s, 7u);
+                put_byte(node.w + 20, s, 1u);
+                put_byte(node.w + 22, s, 24u + (uint32_t)s);
                 work.push_back({next_child++, kids[kid_in[s]], W.level + 1});
             }
         }

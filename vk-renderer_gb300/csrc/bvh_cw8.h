@@ -21,22 +21,24 @@ namespace vkt {
 //            interior children are stored consecutively in slot order
 //   w5       prim_base: index (in the 8-wide primitive order) of the first
 //            primitive of the node's leaf children, stored consecutively in
-//            slot order
-//   w6, w7   meta byte of slot k (byte k % 4 of w6 + k / 4):
-//              0            empty slot
-//              c << 5 | o   leaf of c primitives (1..6) at prim_base + o
-//                           (o + c <= 24 for every leaf of the node)
-//              7 << 5       interior child
+//            slot order (at most 24 per node)
+//   w6, w7   octant mask byte of slot k (byte k % 4 of w6 + k / 4): 7 for an
+//            interior child, else 0
 //   w8..w19  quantised box bytes, slot k in byte k % 4 of the word pair:
 //            lo x (w8, w9), lo y (w10, w11), lo z (w12, w13),
 //            hi x (w14, w15), hi y (w16, w17), hi z (w18, w19);
 //            box = [p + lo * 2^(e - 127), p + hi * 2^(e - 127)] per axis,
 //            which contains the binary child's (padded) box exactly
-//   w20..w23 zero
-// Slot order: slot s (s = sign bits of a ray direction, bit a set for a
-// negative component on axis a) holds the child met first by rays of that
-// octant; a ray of octant s visits the hit interior children in descending
-// order of slot ^ s ^ 7.
+//   w20, w21 hit-mask bits of slot k: a leaf of c primitives (1..6) ->
+//            (1 << c) - 1; an interior child -> 1; an empty slot -> 0
+//   w22, w23 bit position of slot k: a leaf -> o, its first primitive being
+//            prim_base + o (o + c <= 24); an interior child -> 24 + slot
+// A child hit by a ray of octant s (bit a set for a negative direction
+// component on axis a) adds its bits at position (position ^ (mask & s ^ 7)):
+// the primitives to test in bits 0..23, the interior children in bits 24..31,
+// slot k at bit 24 + (k ^ s ^ 7).  Slot order: slot s holds the child met
+// first by rays of octant s; the traversal visits the hit interior children
+// highest bit first, i.e. in descending order of slot ^ s ^ 7.
 struct alignas(32) Cw8Node {
     uint32_t w[24];
 };

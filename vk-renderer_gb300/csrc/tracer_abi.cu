@@ -858,6 +858,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         r = pick_width(c, p, wstack, wc.wide);
         if (r != TRACER_OK) return r;
         a.stack_depth = wstack;
+        if (wc.wide != WF_WIDTH_8) a.sc.tri_cw8 = a.sc.tri_cw8_prims = nullptr;  // finishing kernel: binary too
         r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, p->tail_paths, st);
         if (r != TRACER_OK) return r;
     }
@@ -1106,7 +1107,7 @@ extern "C" int tracer_trace_noalloc(tracer_ctx* c, const tracer_frame* f, const 
     std::memset(&a, 0, sizeof a);
     a.sc = DevScene{s.tri.p, s.mats.p, s.sph_geo.p, s.sph_id.p, s.sph_rec.p, s.planes.p, s.emit.p, s.tri_nodes.p,
                     s.sph_nodes.p, s.nt, s.nm, s.ns, s.np, s.ne, s.n_tri_nodes, s.n_sph_nodes,
-                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p, s.tri_cw8.p, s.tri_cw8_prims.p};
+                    s.tri_wide.p, s.sph_wide.p, s.tri_enc.p, s.sph_enc.p, nullptr, nullptr};  // binary traversal only
     a.fr.aspect = f->aspect_ratio;
     a.fr.seed = f->seed;
     a.fr.cpos = V3{f->camera.pos[0], f->camera.pos[1], f->camera.pos[2]};
@@ -1501,6 +1502,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         TraceArgs& a = slots[k];
         std::memset(&a, 0, sizeof a);
         a.sc = c->batch_scenes[k];
+        if (wide != WF_WIDTH_8) a.sc.tri_cw8 = a.sc.tri_cw8_prims = nullptr;  // finishing kernel: binary too
         a.fr.aspect = f.aspect_ratio;
         a.fr.seed = f.seed;
         a.fr.cpos = V3{f.camera.pos[0], f.camera.pos[1], f.camera.pos[2]};
@@ -1790,6 +1792,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         r = pick_width(c, p, wstack, wc.wide);
         if (r != TRACER_OK) return r;
         a.stack_depth = wstack;
+        if (wc.wide != WF_WIDTH_8) a.sc.tri_cw8 = a.sc.tri_cw8_prims = nullptr;
         const AdjWf aw{dldi, lin, ab.grad.p, s.nm, ab.pix.p};
         c->last_kernel = TRACER_KERNEL_WAVEFRONT;
         c->last_launches = 1;  // + generate, rounds; the FP64-to-float conversion

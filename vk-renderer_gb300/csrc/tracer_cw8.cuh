@@ -29,9 +29,13 @@ __device__ __forceinline__ Cw8Ray make_cw8ray(const Ray& r)
     return c;
 }
 
+// Byte k of w as a float, exactly: the byte placed in the low mantissa of
+// 2^23 (one byte permute: 0x4B0000bb = 2^23 + b), minus 2^23.  Two full-rate
+// instructions instead of an integer-to-float conversion, whose pipe is a
+// fraction of the FMA pipe's width (a node visit converts 48 bytes).
 __device__ __forceinline__ float ubyte_f(uint32_t w, int k)
 {
-    return __uint2float_rn((w >> (8 * k)) & 0xFFu);
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)k)) - 8388608.0f;
 }
 
 // Visits node `idx`: tests its children's boxes against the ray with the
@@ -62,16 +66,18 @@ __device__ __forceinline__ void cw8_visit(const float4* nodes, uint32_t idx, con
     // near / far plane words per axis (two words = eight slots)
     const bool fx = r.br.ix < 0.0f, fy = r.br.iy < 0.0f, fz = r.br.iz < 0.0f;
     // b = w8..w15: lo x (b0, b1), lo y (b2, b3), lo z (b4, b5), hi x (b6, b7)
-    // c = w16..w23: hi y (c0, c1), hi z (c2, c3)
+    // c = w16..w23: hi y (c0, c1), hi z (c2, c3), bits (c4, c5), positions (c6, c7)
     const uint32_t lox[2] = {b[0], b[1]}, loy[2] = {b[2], b[3]}, loz[2] = {b[4], b[5]};
     const uint32_t hix[2] = {b[6], b[7]}, hiy[2] = {c[0], c[1]}, hiz[2] = {c[2], c[3]};
-    uint32_t hits = 0, prims = 0;
+    const uint32_t oct4 = r.oct7 * 0x01010101u;
+    uint32_t mask = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const uint32_t qnx = fx ? hix[h] : lox[h], qfx = fx ? lox[h] : hix[h];
         const uint32_t qny = fy ? hiy[h] : loy[h], qfy = fy ? loy[h] : hiy[h];
         const uint32_t qnz = fz ? hiz[h] : loz[h], qfz = fz ? loz[h] : hiz[h];
-        const uint32_t meta = a[6 + h];
+        const uint32_t bits4 = c[4 + h];
+        const uint32_t pos4 = c[6 + h] ^ (oct4 & a[6 + h]);  // interior children: slot ^ s ^ 7
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const float tnx = __fmaf_rn(ubyte_f(qnx, k), ax, bx);
@@ -82,19 +88,12 @@ __device__ __forceinline__ void cw8_visit(const float4* nodes, uint32_t idx, con
             const float tfz = __fmaf_rn(ubyte_f(qfz, k), az, bz);
             const float tmin = fmaxf(fmax3(tnx, tny, tnz), 0.0f);
             const float tmax = fminf(fmin3(tfx, tfy, tfz), tbest);
-            const uint32_t m = (meta >> (8 * k)) & 0xFFu;
-            if (tmin <= tmax * BOX_SLACK) {
-                const uint32_t cnt = m >> 5;
-                const int slot = 4 * h + k;
-                if (cnt == 7u)
-                    hits |= 1u << (24 + (slot ^ r.oct7));
-                else
-                    prims |= ((1u << cnt) - 1u) << (m & 31u);
-            }
+            if (tmin <= tmax * BOX_SLACK)
+                mask |= __byte_perm(bits4, 0u, 0x4440u | (uint32_t)k) << __byte_perm(pos4, 0u, 0x4440u | (uint32_t)k);
         }
     }
-    G = make_uint2(a[4], hits | (a[3] >> 24));
-    P = make_uint2(a[5], prims);
+    G = make_uint2(a[4], (mask & 0xFF000000u) | (a[3] >> 24));
+    P = make_uint2(a[5], mask & 0x00FFFFFFu);
 }
 
 // Takes the next child of a node group (which has one): its node index; the
@@ -108,17 +107,17 @@ __device__ __forceinline__ uint32_t cw8_next(uint2& G, uint32_t oct7)
 }
 
 // Tests primitive k of the 8-wide order: a 64-byte record
-// (v0, original id) (v1 - v0, leaf-ordered slot) (v2 - v0, 0) (0), read as two
-// 256-bit loads; on acceptance the hit records the leaf-ordered slot (the
-// storage slot every other kernel indexes).
+// (v0, original id) (v1 - v0, leaf-ordered slot) (v2 - v0, 0) (0), read as a
+// 256-bit and a 128-bit load (the last 16 bytes are padding); on acceptance
+// the hit records the leaf-ordered slot (the storage slot every other kernel
+// indexes).
 template <bool STATS>
 __device__ __forceinline__ void cw8_test_tri(const float4* tris, uint32_t k, const Ray& ray, Hit& h, Counters& cnt)
 {
     if (STATS) cnt.c[C_TRIS]++;
-    float4 ta, tb, tc, td;
+    float4 ta, tb;
     ldg256(tris + 4 * (size_t)k, ta, tb);
-    ldg256(tris + 4 * (size_t)k + 2, tc, td);
-    (void)td;
+    const float4 tc = __ldg(tris + 4 * (size_t)k + 2);
     const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
     const uint32_t id = __float_as_uint(ta.w);
     if (accept_strict(tt, id, h)) {
@@ -127,6 +126,66 @@ __device__ __forceinline__ void cw8_test_tri(const float4* tris, uint32_t k, con
         h.kind = 1;
         h.slot = __float_as_uint(tb.w);
     }
+}
+
+// Closest hit of one ray by one thread over the 8-wide BVH of a
+// triangle-only scene, for the finishing kernel: the extend kernel's node
+// visit and triangle test (strict ties), without the warp's phases -- a
+// node's leaves are tested right after the visit -- so the same hit.  h.t
+// holds tmax on entry; on a miss h.kind = 0 and h.prim = NO_PRIM.  stk: the
+// thread's stack of node groups (8-byte entries, interleaved by thread).
+template <bool STATS>
+__device__ __forceinline__ bool closest_cw8(const DevScene& sc, const Ray& ray, Hit& h, const PairStack& stk,
+                                            int* status, uint32_t trav_limit, Counters& cnt)
+{
+    if (STATS) cnt.c[C_CLOSEST]++;
+    Hit b;
+    b.t = h.t;
+    b.prim = 0;  // see accept_strict
+    b.kind = 0;
+    b.slot = 0;
+    if (!isnan3(ray.d)) {
+        if (sc.n_tri_nodes > 0 && sc.nt > 0) {
+            const Cw8Ray cr = make_cw8ray(ray);
+            uint2 G = make_uint2(0u, (1u << (24 + (0u ^ cr.oct7))) | 1u);
+            int sp = 0;
+            uint32_t steps = 0;
+            for (;;) {
+                if ((G.y & 0xFF000000u) == 0u) {
+                    if (sp == 0) break;
+                    --sp;
+                    const int2 e = stk.e[sp * stk.stride];
+                    G = make_uint2((uint32_t)e.x, (uint32_t)e.y);
+                }
+                if (++steps > trav_limit) {
+                    atomicCAS(status, ST_OK, ST_TRAVERSAL_LIMIT);
+                    break;
+                }
+                const uint32_t idx = cw8_next(G, cr.oct7);
+                if (G.y & 0xFF000000u) {
+                    if (sp >= stk.cap) {
+                        atomicCAS(status, ST_OK, ST_STACK_OVERFLOW);
+                    } else {
+                        stk.e[sp * stk.stride] = make_int2((int)G.x, (int)G.y);
+                        ++sp;
+                    }
+                }
+                uint2 P;
+                cw8_visit(sc.tri_cw8, idx, cr, b.t, G, P);
+                if (STATS) cnt.c[C_NODES] += 3;
+                for (uint32_t m = P.y; m != 0u; m &= m - 1u)
+                    cw8_test_tri<STATS>(sc.tri_cw8_prims, P.x + (uint32_t)(__ffs(m) - 1), ray, b, cnt);
+            }
+        }
+        planes_pass<STATS>(sc, ray, b, cnt);
+    }
+    h = b;
+    if (h.kind == 0) {
+        h.prim = NO_PRIM;
+        return false;
+    }
+    if (STATS) cnt.c[C_HITS]++;
+    return true;
 }
 
 }  // namespace vkt

@@ -688,7 +688,9 @@ __global__ void __launch_bounds__(128) wf_finish(TraceArgs a, WfState s, int qse
         for (;;) {
             Hit h;
             h.t = depth_tmax(ps.depth);
-            if (BVH)
+            if (BVH && A.sc.tri_cw8 != nullptr)  // triangle-only scenes with an 8-wide BVH
+                closest_cw8<STATS>(A.sc, ps.ray, h, pstk, a.status, A.trav_limit, cnt);
+            else if (BVH)
                 closest_enc<STATS>(A.sc, ps.ray, h, pstk, a.status, A.trav_limit, cnt);
             else
                 tr.trace(ps.ray, h, false);

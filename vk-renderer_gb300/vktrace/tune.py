@@ -1,12 +1,15 @@
 """Autotuner for the wavefront launch shape.
 
 Sweeps the extend kernel's block size, the traversal stack depth (0 = the
-bound the BVH needs), the traversal width (4-wide or binary nodes) and the
-"wavefront size" (resident extend CTAs per SM, i.e. how many rays are in
-flight at once), timing each candidate on the device with CUDA events
-(tracer_last_timings), and returns the fastest.  Candidates the library
-refuses (a stack shallower than the BVH, a shape that cannot be resident)
-are recorded as skipped.  Results are deterministic given the timings.
+bound the BVH needs), the traversal width (compressed 8-wide, 4-wide or
+binary nodes) and the "wavefront size" (resident extend CTAs per SM, i.e.
+how many rays are in flight at once), timing each candidate on the device
+with CUDA events (tracer_last_timings); then times the `refine` fastest
+candidates again, `refine_reps` times each, and returns the one with the
+smallest median, so that one noisy sample does not pick the launch shape.
+Candidates the library refuses (a stack shallower than the BVH, a shape that
+cannot be resident, a width the scenes lack) are recorded as skipped.
+Results are deterministic given the timings.
 """
 from __future__ import annotations
 
@@ -22,12 +25,13 @@ def _set(params, block, stack, wave, width, tail=0):
 
 
 def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stacks=(0, 16, 32, 64),
-                     wavefronts=(0, 6, 4), widths=(4, 2), tails=(0,), reps: int = 1, use_graph: bool = True,
-                     budget_s: float = 60.0):
+                     wavefronts=(0, 6, 4), widths=(8, 4, 2), tails=(0,), reps: int = 1, use_graph: bool = True,
+                     budget_s: float = 60.0, refine: int = 3, refine_reps: int = 5):
     """Returns (best, table): best = dict(block, stack_depth, wavefront,
     bvh_width, tail_paths, ms); table = one dict per candidate (ms or
-    skipped reason).  tails: tail_paths values (live paths below which the
-    rest goes to the finishing kernel; 0 = the library's choice)."""
+    skipped reason; the re-timed ones also ms_refined).  tails: tail_paths
+    values (live paths below which the rest goes to the finishing kernel;
+    0 = the library's choice)."""
     table = []
     best = None
     t_start = time.perf_counter()
@@ -55,6 +59,20 @@ def autotune_batched(tr: abi.Tracer, frames, params, blocks=(64, 128, 256), stac
             table.append(row)
             if best is None or ms < best["ms"]:
                 best = dict(row)
+        # second stage: the fastest few again, several times each
+        timed = sorted((r for r in table if "ms" in r), key=lambda r: r["ms"])[:max(0, refine)]
+        if len(timed) > 1 and refine_reps > 0:
+            for row in timed:
+                _set(params, row["block"], row["stack_depth"], row["wavefront"], row["bvh_width"], row["tail_paths"])
+                tr.trace_batched(frames, params, use_graph=use_graph)
+                tr.synchronize()
+                times = []
+                for _ in range(refine_reps):
+                    tr.trace_batched(frames, params, use_graph=use_graph)
+                    times.append(tr.timings()["total_ms"])
+                row["ms_refined"] = sorted(times)[len(times) // 2]
+            top = min(timed, key=lambda r: r["ms_refined"])
+            best = dict(top, ms=top["ms_refined"])
     finally:
         tr.set_profiling(False)
         for p, (b, s, w, wd, tl) in zip(params, saved):
