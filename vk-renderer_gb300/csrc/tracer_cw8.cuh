@@ -29,13 +29,13 @@ __device__ __forceinline__ Cw8Ray make_cw8ray(const Ray& r)
     return c;
 }
 
-// Byte k of w as a float, exactly: the byte placed in the low mantissa of
-// 2^23 (one byte permute: 0x4B0000bb = 2^23 + b), minus 2^23.  Two full-rate
-// instructions instead of an integer-to-float conversion, whose pipe is a
-// fraction of the FMA pipe's width (a node visit converts 48 bytes).
+// Byte k of w as a float (exact).  An integer-to-float conversion: the
+// kernel's busiest pipe is the integer ALU (58 % in ncu), and the
+// conversion's pipe is another one; a byte permute into 2^23 + b minus 2^23
+// (ALU + FMA) measured slower on c1 (71.8 against 69.1 ms per frame).
 __device__ __forceinline__ float ubyte_f(uint32_t w, int k)
 {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)k)) - 8388608.0f;
+    return __uint2float_rn((w >> (8 * k)) & 0xFFu);
 }
 
 // Visits node `idx`: tests its children's boxes against the ray with the

@@ -352,8 +352,9 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
 }
 
 // Primitive groups a lane of the 8-wide traversal may hold back while the
-// warp's slowest lane is still looking for its first.
-constexpr int kCw8Postpone = 2;
+// warp's slowest lane is still looking for its first (c1 frame, ms: 1 ->
+// 100.8, 2 -> 69.1, 4 -> 61.1, 6 -> 60.9, 8 -> 61.1, 12 -> 63.1).
+constexpr int kCw8Postpone = 6;
 
 // The extend kernel over the compressed 8-wide BVH (triangle scenes; strict
 // ties).  Same phases as wf_extend_bvh: idle lanes fetch rays; all lanes visit
