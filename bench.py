@@ -136,7 +136,8 @@ def aggregate(world: int, rays: float, seconds: float, device: str = "cuda"):
     return r.item() / t.item() / 1e6, t.item(), r.item()
 
 
-TRAVERSAL_LABEL = {0: "auto (= binary)", 2: "binary", 4: "4-wide"}
+TRAVERSAL_LABEL = {0: "auto (= compressed 8-wide for triangle-only scenes)", 2: "binary", 4: "4-wide",
+                   8: "compressed 8-wide"}
 
 
 def workload_config(wl, world: int) -> dict:
@@ -264,9 +265,11 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
     ms_plain = timed(p_plain, False)
     plain_imgs = [tr.readback_scene(k, abi.AOV_RGBA32F) for k in range(len(wls))]
     p_wf = prm(abi.KERNEL_WAVEFRONT, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F))
-    # binary traversal only (4-wide measured slower on these soups); the
+    # the compressed 8-wide and the binary traversal (the uncompressed 4-wide
+    # measured slower on these soups), the stack the BVHs need, the
     # finishing kernel's threshold: the library's choice or 1M live paths
-    best, table = tune.autotune_batched(tr, frames, p_wf, widths=(2,), tails=(0, 1_000_000), budget_s=40.0)
+    best, table = tune.autotune_batched(tr, frames, p_wf, widths=(8, 2), blocks=(128, 256), stacks=(0,),
+                                        wavefronts=(0, 6), tails=(0, 1_000_000), budget_s=40.0)
     for p in p_wf:
         p.block, p.stack_depth, p.wavefront = best["block"], best["stack_depth"], best["wavefront"]
         p.bvh_width, p.tail_paths = best["bvh_width"], best["tail_paths"]
@@ -277,6 +280,7 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
         b = plain_imgs[k][:, 1:, :3].astype(np.float64)
         rmse = max(rmse, float(np.sqrt(np.mean((a - b) ** 2))))
     tr.close()
+    decomp = batch_decomposition(local, wls, p_plain)
     pixels = sum(w.pixels for w in wls)
     return {"metric": "batched Mrays/s (64 scenes, one CUDA-graph wavefront)", "value": rays / (ms_wf / 1e3) / 1e6,
             "unit": UNIT, "ms_per_step": ms_wf,
@@ -286,8 +290,53 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
             "max_image_rmse_vs_plain": rmse, "rays_per_step": rays, "scenes": len(wls), "pixels": pixels,
             "triangles": int(sum(len(w.scene.triangles) for w in wls)),
             "autotuned": best, "autotune_candidates": len(table),
+            "decomposition": decomp,
             "config": {"workload": "c2-64scenes-tris-loguniform-1k-200k-res128-1024-4spp-d6-rr3-sah16",
                        "l2": "flushed before each timed step (256 MiB write)"}}
+
+
+def batch_decomposition(local: int, wls, p_plain) -> dict:
+    """Where the batch's speed-up over one plain launch per scene comes from:
+    every scene traced on its own (its own upload, one tracer_trace) with the
+    plain kernel and with the wavefront (the library's defaults: automatic
+    width and hand-over), device-timed (median of 3, L2 flushed), against
+    the batch.  plain -> wavefront per scene is the kernels' gain; the rest is
+    the batch's (one queue filling the GPU across scenes, one tail, no
+    per-scene launches).  Also split by image size."""
+    import torch
+    from vktrace import abi
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    tr = abi.Tracer(local)
+    rows = []
+    for k, w in enumerate(wls):
+        tr.upload_scene(w.scene)
+        pw = abi.Tracer.params(w.width, w.height, spp=w.spp, max_depth=w.max_depth, rr_start=w.rr_start, sky=w.sky,
+                               kernel=abi.KERNEL_WAVEFRONT, aovs=(abi.AOV_RGBA8, abi.AOV_RGBA32F))
+        ms = {}
+        for name, p in (("plain", p_plain[k]), ("wavefront", pw)):
+            tr.trace(w.frame, p, sptr)
+            times = []
+            for _ in range(3):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                tr.trace(w.frame, p, sptr)
+                b.record(stream)
+                torch.cuda.synchronize()
+                tr.synchronize()
+                times.append(a.elapsed_time(b))
+            ms[name] = sorted(times)[1]
+        rows.append((w.width, len(w.scene.triangles), ms["plain"], ms["wavefront"]))
+    tr.close()
+    out = {"plain_single_ms": sum(r[2] for r in rows), "wavefront_single_ms": sum(r[3] for r in rows),
+           "by_resolution": {}}
+    for res in sorted({r[0] for r in rows}):
+        sel = [r for r in rows if r[0] == res]
+        out["by_resolution"][f"{res}^2"] = {"scenes": len(sel), "plain_ms": sum(r[2] for r in sel),
+                                            "wavefront_ms": sum(r[3] for r in sel)}
+    return out
 
 
 def _perturbed_albedo(mats, seed, sigma=0.1):
@@ -397,6 +446,7 @@ def adjoint_section(local: int, steps: int) -> dict:
         rel_r.append(abs(g_alb[m, c] - fr) / abs(fr))
     tr.set_materials(base)
     fp64 = fp64_host_check(wl, target, g_alb, idx)
+    campos = campos_check(tr, wl, p_run)
     tr.close()
     fwd = fwd_rays / (ms_fwd / 1e3) / 1e6
     # headline: the forward frame's rays per second of adjoint time, i.e.
@@ -414,9 +464,94 @@ def adjoint_section(local: int, steps: int) -> dict:
             "kernels": per_kernel,
             "grad_check": {"max_rel_err_vs_central_fd": max(rel), "step": 1e-3,
                            "max_rel_err_vs_richardson_fd": max(rel_r), "steps": [1e-3, 5e-4],
-                           "components": len(rel), "fp64_host": fp64},
+                           "components": len(rel), "fp64_host": fp64, "camera_position": campos},
             "loss": L0,
             "config": {"workload": wl.name, "triangles": len(wl.scene.triangles), "materials": nm}}
+
+
+def campos_check(tr, wl, p) -> dict:
+    """The camera-position gradient at c3 (its boundary part: triangle
+    outlines moving across the point-sampled pixels) against central
+    differences of the GPU forward with common random numbers, for a linear
+    loss (fixed random weights per pixel, so dL/dI is exact at every camera
+    position), step h = 0.02, averaged over 16 x 16 sub-pixel offsets of every
+    sample point (the camera's dir moved along right and up by a fraction of
+    a pixel: the one-pixel box the boundary term differentiates).  The
+    differences count outline crossings of sample points; their standard
+    error comes from the spread of 16 interleaved subsets of the offsets,
+    and err_in_se is the gradient's distance from them in units of it.
+    Also the adjoint's time with the boundary part on."""
+    import numpy as np
+    from vktrace import abi
+    from vktrace import scene as S
+    g = np.random.default_rng(5)
+    dl = np.zeros((wl.height, wl.width, 4), np.float32)
+    dl[:, 1:, :3] = g.normal(size=(wl.height, wl.width - 1, 3)).astype(np.float32)
+    p.aov_mask = (1 << abi.AOV_RGBA32F) | (1 << abi.AOV_LINEAR)
+    tr.trace(wl.frame, p)
+    lin = tr.readback(abi.AOV_LINEAR)
+    # the adjoint with the boundary part on (4 pieces per edge), device-timed
+    # with every input resident
+    import torch
+    nm = len(wl.scene.materials)
+    dl_d, lin_d = torch.from_numpy(dl).cuda(), torch.from_numpy(lin).cuda()
+    outs = [torch.zeros((nm, 3), device="cuda"), torch.zeros((nm, 3), device="cuda"), torch.zeros(3, device="cuda")]
+    stream = torch.cuda.current_stream()
+    tr.set_edge_sampling(4)
+    try:
+        call = lambda: tr.trace_adjoint(wl.frame, p, dl_d.data_ptr(), lin_d.data_ptr(),
+                                        outputs=tuple(o.data_ptr() for o in outs), stream=stream.cuda_stream)
+        for _ in range(2):
+            call()
+        tr.synchronize()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(5):
+            call()
+        b.record(stream)
+        torch.cuda.synchronize()
+        tr.synchronize()
+        ms_edges = a.elapsed_time(b) / 5
+        _, _, gc = tr.trace_adjoint(wl.frame, p, dl, lin, num_materials=nm)
+    finally:
+        tr.set_edge_sampling(0)
+    h, ks = 0.02, 16
+    out = {"loss": "linear, N(0,1) weights per pixel and channel", "step": h, "subpixel_offsets": ks * ks,
+           "gradient": [float(v) for v in gc], "fd": [], "standard_error": [], "events": [], "err_in_se": [],
+           "adjoint_ms_with_boundary_part": ms_edges,
+           "note": "boundary part on (tracer_set_edge_sampling 4; off by default): primary-visibility edge "
+                   "sampling; outlines seen only by bounce rays are not modelled"}
+    base = np.array(wl.frame, S.FRAME).reshape(())
+    pos0 = np.array(base["camera"]["pos"], np.float64)
+    for axis in range(3):
+        step = float(np.float32(pos0[axis] + h) - np.float32(pos0[axis] - h))
+        per = np.zeros((ks, ks))
+        ev = 0
+        for i in range(ks):
+            for j in range(ks):
+                ox, oy = (i + 0.5) / ks - 0.5, (j + 0.5) / ks - 0.5
+                imgs = []
+                for sgn in (1.0, -1.0):
+                    f = base.copy()
+                    pos = pos0.copy()
+                    pos[axis] += sgn * h
+                    f["camera"]["pos"] = pos.astype(np.float32)
+                    cam = f["camera"]
+                    cam["dir"] = (cam["dir"].astype(np.float64) + cam["right"] * (2.0 * ox / wl.width)
+                                  + cam["up"] * (2.0 * oy / wl.height)).astype(np.float32)
+                    tr.trace(f, p)
+                    imgs.append(tr.readback(abi.AOV_RGBA32F))
+                d = ((imgs[0][:, 1:, :3].astype(np.float64) - imgs[1][:, 1:, :3]) * dl[:, 1:, :3]).sum(-1) / step
+                per[i, j] = d.sum()
+                ev += int((d != 0).sum())
+        subs = [per[a::4, b::4].mean() for a in range(4) for b in range(4)]
+        fd, se = float(per.mean()), float(np.std(subs, ddof=1) / 4.0)
+        out["fd"].append(fd)
+        out["standard_error"].append(se)
+        out["events"].append(ev)
+        out["err_in_se"].append(abs(float(gc[axis]) - fd) / se if se > 0 else None)
+    return out
 
 
 def fp64_host_check(wl, target, g_alb, idx) -> dict:
@@ -864,7 +999,8 @@ def run_ours(args):
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (NCU_EXTEND_DRAM_BYTES_PER_RAY * rays
                                      if kern == abi.KERNEL_WAVEFRONT else None),
-                         "kernel": ("wf_extend_bvh (+ wf_finish for the last paths)" if kern == abi.KERNEL_WAVEFRONT
+                         "kernel": (("wf_extend_cw8" if args.bvh_width in (0, 8) else "wf_extend_bvh")
+                                    + " (+ wf_finish for the last paths)" if kern == abi.KERNEL_WAVEFRONT
                                     else "k_plain"),
                          "algorithmic_bytes_per_frame": k_bytes, "kernel_ms_per_frame": k_ms,
                          "launches_per_frame": breakdown["rounds"] if kern == abi.KERNEL_WAVEFRONT else 1,
@@ -908,8 +1044,9 @@ def main():
     ap.add_argument("--kernel", choices=["wavefront", "plain"], default="wavefront")
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--wavefront", type=int, default=0)
-    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4],
-                    help="wavefront traversal: 0 auto (= binary), 2 binary, 4 4-wide")
+    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4, 8],
+                    help="wavefront traversal: 0 auto (= 8-wide for triangle-only scenes), 2 binary, 4 4-wide, "
+                         "8 compressed 8-wide")
     ap.add_argument("--tail-paths", type=int, default=0,
                     help="wavefront hand-over to the finishing kernel below this many live paths (0 auto, 1 never)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

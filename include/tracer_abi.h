@@ -273,10 +273,29 @@ int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* byt
  * waits (bounded) for the result, with device outputs it is asynchronous on
  * cuda_stream.  Path replay: every sample is traced twice more (no path
  * vertices are stored); the Russian-roulette normalisation is treated as a
- * constant.  Materials of spheres and planes (stored inline) get no gradient. */
+ * constant.  Materials of spheres and planes (stored inline) get no gradient.
+ * d_campos is the interior part (the camera position enters next-event
+ * shading through the view vector and the hit points: the derivative of the
+ * point-sampled image away from outlines, zero for scenes without emissive
+ * spheres) plus, when tracer_set_edge_sampling has turned it on, the boundary
+ * part: the image changes as triangle outlines move across pixels, which is
+ * the derivative of each pixel averaged over a one-pixel box around its
+ * sample point (edge sampling of primary visibility; outlines seen only by
+ * bounce rays, and sphere outlines, are not included).  The boundary part
+ * re-evaluates every pixel an outline crosses on both sides of it, which on
+ * the 10k-triangle soup at 256^2 x 4 spp costs about three times the rest of
+ * the adjoint. */
 int tracer_trace_adjoint(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
                          const float* dL_dimage, const float* linear_image, float* d_albedo, float* d_emission,
                          float* d_campos, void* cuda_stream);
+
+/* Turns on the boundary part of d_campos in tracer_trace_adjoint and sets
+ * how many pieces each triangle edge's image is split into (one GPU thread
+ * each; each piece is integrated exactly over the pixel boxes it crosses, so
+ * this is a parallelism setting, 4 being a good value); 0 = off, the
+ * default.  At most 1024.  Applies to every later adjoint of the context.
+ * No counterpart in the reference. */
+int tracer_set_edge_sampling(tracer_ctx* ctx, uint32_t samples_per_edge);
 
 /* ------------------------------------------------------------ batches
  * Many independent scenes of uneven size and resolution traced together (no

@@ -77,7 +77,7 @@ def test_adjoint_vs_central_fd_gpu(gpu_tracer):
     target, _ = _render(tr, sc, fr, p, tgt_m)
     img, lin = _render(tr, sc, fr, p, base)
     L0, dl = _loss_and_dl(img, target)
-    ga, ge, gc = tr.trace_adjoint(fr, p, dl, lin, num_materials=len(base))
+    ga, ge, gc = tr.trace_adjoint(fr, p, dl, lin, num_materials=len(base))  # the interior part alone
     assert np.all(gc == 0.0)  # no emitters: radiance does not depend on the camera away from edges
     # albedo: the stated step 1e-3.  Emission: diffuse emission enters as
     # normalize(e) with |e| ~ 0.03, whose curvature (and the acc clamp it
@@ -169,7 +169,8 @@ def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case):
     _, dl = _loss_and_dl(img, target)
     out = {}
     # wavefront: rounds to the end (tail 1), the finishing kernel right after
-    # generate (tail 2^32 - 1), and a hand-over part-way (700)
+    # generate (tail 2^32 - 1), and a hand-over part-way (700); the interior
+    # part of the camera gradient (edge sampling off, the default), zero without emitters
     for k, tail in ((abi.KERNEL_PLAIN, 0), (abi.KERNEL_WAVEFRONT, 1), (abi.KERNEL_WAVEFRONT, 0xFFFFFFFF),
                     (abi.KERNEL_WAVEFRONT, 700)):
         p.kernel = k
@@ -231,6 +232,9 @@ def test_camera_and_nee_gradients_vs_fp64(gpu_tracer, kind):
     target = tr.readback(abi.AOV_RGBA32F)
     img, lin = _render(tr, sc, fr, p)
     _, dl = _loss_and_dl(img, target)
+    # the interior part (edge sampling off, the default; the differences below
+    # exclude pixels whose visible primitive changes); the boundary part has
+    # tests of its own
     ga, ge, gc = tr.trace_adjoint(fr, p, dl, lin, num_materials=1)
     prm = pyoracle.params(w, h, spp=1, max_depth=1, rr_start=1, tie_mode=1)
     prm_f = pyoracle.params(w, h, spp=1, max_depth=1, rr_start=1, tie_mode=1)

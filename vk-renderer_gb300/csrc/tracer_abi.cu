@@ -14,6 +14,7 @@
 #include <cstring>
 #include <string>
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <mutex>
 #include <thread>
@@ -23,6 +24,7 @@
 
 #include "tracer_abi.h"
 #include "tracer_core.cuh"
+#include "tracer_edges.h"
 #include "tracer_launch.h"
 #include "tracer_present.h"
 #include "bvh_cw8.h"
@@ -163,6 +165,7 @@ struct tracer_ctx {
     uint64_t acc_version = 0;
     DevBuf<unsigned char> pres_src[2], pres_out;  // staging for host images
     uint32_t trav_cap = 0;            // tracer_set_traversal_limit: 0 = automatic
+    uint32_t edge_samples = 0;        // tracer_set_edge_sampling: pieces per triangle edge, 0 = off
 };
 
 namespace {
@@ -442,6 +445,26 @@ uint32_t trav_limit(const tracer_ctx* c, uint32_t nodes)
     return c->trav_cap ? c->trav_cap : 2 * nodes + 16;
 }
 
+// Inverse of the matrix with columns dir, right, up (row-major), for the
+// image projection of the camera's boundary term; false if singular.
+bool camera_inverse(const tracer_camera& cam, float out[9])
+{
+    const double m[3][3] = {{cam.dir[0], cam.right[0], cam.up[0]},
+                            {cam.dir[1], cam.right[1], cam.up[1]},
+                            {cam.dir[2], cam.right[2], cam.up[2]}};
+    const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                       m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                       m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    if (!(std::fabs(det) > 1e-12)) return false;
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 3; ++k) {
+            // cofactor of (k, r) / det
+            const int r0 = (k + 1) % 3, r1 = (k + 2) % 3, c0 = (r + 1) % 3, c1 = (r + 2) % 3;
+            out[3 * r + k] = (float)((m[r0][c0] * m[r1][c1] - m[r0][c1] * m[r1][c0]) / det);
+        }
+    return true;
+}
+
 int pick_width(tracer_ctx* c, const tracer_trace_params* p, uint32_t& stack, int& wide)
 {
     const SceneBuffers& s = c->scene;
@@ -602,6 +625,14 @@ int tracer_set_traversal_limit(tracer_ctx* c, uint32_t steps)
     int r = finish(c);
     if (r != TRACER_OK) return r;
     c->trav_cap = steps;
+    return TRACER_OK;
+}
+
+int tracer_set_edge_sampling(tracer_ctx* c, uint32_t samples_per_edge)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    if (samples_per_edge > 1024) return fail(c, TRACER_ERR_INVALID_ARG, "at most 1024 samples per edge");
+    c->edge_samples = samples_per_edge;
     return TRACER_OK;
 }
 
@@ -1805,6 +1836,15 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         c->last_launches = 2;  // adjoint + FP64-to-float conversion
         if (c->profiling) cudaEventRecord(c->prof_begin, st);
         e = launch_adjoint(a, dldi, lin, ab.grad.p, s.nm, p->tie_mode, s.bvh ? 1 : 0, st);
+    }
+    // the camera's boundary term: triangle outlines moving across pixels
+    if (e == cudaSuccess && d_campos && s.nt > 0 && c->edge_samples > 0) {
+        EdgeArgs ea{dldi, ab.grad.p + 6 * (size_t)s.nm, {}, c->edge_samples, 0.01f};
+        if (!camera_inverse(f->camera, ea.binv)) return fail(c, TRACER_ERR_INVALID_ARG, "degenerate camera basis");
+        TraceArgs ae = a;
+        ae.stack_depth = stack;  // the binary traversal's
+        e = launch_edge_campos(ae, ea, p->tie_mode, s.bvh ? 1 : 0, st);
+        c->last_launches += 1;
     }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
     if (e == cudaSuccess) e = launch_grad_to_float(ab.grad.p, ab.gradf.p, (uint32_t)ng, st);

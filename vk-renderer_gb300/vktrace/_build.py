@@ -29,10 +29,11 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall"]
 
-SOURCES = ["tracer_kernels.cu", "tracer_wavefront.cu", "tracer_adjoint.cu", "tracer_present.cu", "tracer_whitted.cu",
+SOURCES = ["tracer_kernels.cu", "tracer_wavefront.cu", "tracer_adjoint.cu", "tracer_edges.cu", "tracer_present.cu",
+           "tracer_whitted.cu",
            "tracer_abi.cu", "bvh_build.cpp", "bvh_wide.cpp", "bvh_cw8.cpp", "camera.cpp"]
 HEADERS = ["tracer_device.cuh", "tracer_core.cuh", "tracer_traverse.cuh", "tracer_launch.h", "tracer_wavefront.h",
-           "tracer_present.h", "tracer_cw8.cuh",
+           "tracer_present.h", "tracer_cw8.cuh", "tracer_edges.h",
            "bvh_wide.h", "bvh_cw8.h"]
 
 

@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = [
     "tracer_readback_scene", "tracer_trace_adjoint", "tracer_present", "tracer_draw", "tracer_draw_reset",
     "tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update", "tracer_camera_move",
     "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script", "tracer_trace_whitted",
-    "tracer_last_rounds", "tracer_measure_l2_read", "tracer_set_traversal_limit",
+    "tracer_last_rounds", "tracer_measure_l2_read", "tracer_set_traversal_limit", "tracer_set_edge_sampling",
 ]
 PRESENT_PINGPONG, PRESENT_ACCUMULATE = 0, 1
 KEY_W, KEY_S, KEY_A, KEY_D, KEY_R, KEY_F = 1, 2, 4, 8, 16, 32
@@ -127,6 +127,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_status_string.restype = ctypes.c_char_p
     lib.tracer_set_timeout.argtypes = [vp, u32]
     lib.tracer_set_traversal_limit.argtypes = [vp, u32]
+    lib.tracer_set_edge_sampling.argtypes = [vp, u32]
     lib.tracer_upload_scene.argtypes = [vp, ctypes.POINTER(SceneDesc)]
     lib.tracer_set_materials.argtypes = [vp, vp, u32]
     lib.tracer_trace.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp]
@@ -231,6 +232,10 @@ class Tracer:
     def set_traversal_limit(self, steps: int):
         """Cap on BVH traversal steps per ray (0 = automatic)."""
         self._check(self.lib.tracer_set_traversal_limit(self.h, steps))
+
+    def set_edge_sampling(self, samples_per_edge: int):
+        """Pieces per triangle edge of the camera gradient's boundary part (0 = off, the default)."""
+        self._check(self.lib.tracer_set_edge_sampling(self.h, samples_per_edge))
 
     @staticmethod
     def _fill_desc(d: SceneDesc, sc: S.Scene, tri_bvh=None, sphere_bvh=None) -> list:
