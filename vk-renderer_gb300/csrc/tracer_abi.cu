@@ -889,6 +889,7 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         r = pick_width(c, p, wstack, wc.wide);
         if (r != TRACER_OK) return r;
         a.stack_depth = wstack;
+        if (wc.wide == WF_WIDTH_8) wc.cw8_stack = s.cw8_depth;
         if (wc.wide != WF_WIDTH_8) a.sc.tri_cw8 = a.sc.tri_cw8_prims = nullptr;  // finishing kernel: binary too
         r = run_wavefront(c, a, wc, npx, (uint64_t)p->spp * p->max_depth + 1, wstack, p->wavefront, p->tail_paths, st);
         if (r != TRACER_OK) return r;
@@ -1591,6 +1592,7 @@ extern "C" int tracer_trace_batched(tracer_ctx* c, const tracer_frame* frames, c
         wc.has_emitters = c->batch_emitters;
         wc.block = block;
         wc.wide = wide;
+        if (wide == WF_WIDTH_8) wc.cw8_stack = c->batch.cw8_depth;
         wc.slots = c->batch_slots.p;
         wc.nslots = n;
         if (!use_graph) {
@@ -1823,6 +1825,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         r = pick_width(c, p, wstack, wc.wide);
         if (r != TRACER_OK) return r;
         a.stack_depth = wstack;
+        if (wc.wide == WF_WIDTH_8) wc.cw8_stack = s.cw8_depth;
         if (wc.wide != WF_WIDTH_8) a.sc.tri_cw8 = a.sc.tri_cw8_prims = nullptr;
         const AdjWf aw{dldi, lin, ab.grad.p, s.nm, ab.pix.p};
         c->last_kernel = TRACER_KERNEL_WAVEFRONT;

@@ -32,7 +32,9 @@ __device__ __forceinline__ Cw8Ray make_cw8ray(const Ray& r)
 // Byte k of w as a float (exact).  An integer-to-float conversion: the
 // kernel's busiest pipe is the integer ALU (58 % in ncu), and the
 // conversion's pipe is another one; a byte permute into 2^23 + b minus 2^23
-// (ALU + FMA) measured slower on c1 (71.8 against 69.1 ms per frame).
+// (ALU + FMA) measured slower on c1 (71.8 against 69.1 ms per frame), and so
+// did a conversion of the low byte of the shifted word (cvt.rn.f32.u8: 61.8
+// against 60.4).
 __device__ __forceinline__ float ubyte_f(uint32_t w, int k)
 {
     return __uint2float_rn((w >> (8 * k)) & 0xFFu);
@@ -111,21 +113,137 @@ __device__ __forceinline__ uint32_t cw8_next(uint2& G, uint32_t oct7)
 // 256-bit and a 128-bit load (the last 16 bytes are padding); on acceptance
 // the hit records the leaf-ordered slot (the storage slot every other kernel
 // indexes).
+__device__ __forceinline__ float cw8_tri(const float4* tris, uint32_t k, const Ray& ray, uint32_t& id, uint32_t& slot)
+{
+    float4 ta, tb;
+    ldg256(tris + 4 * (size_t)k, ta, tb);
+    const float4 tc = __ldg(tris + 4 * (size_t)k + 2);
+    id = __float_as_uint(ta.w);
+    slot = __float_as_uint(tb.w);
+    return tri_intersect(ray, v3(ta), v3(tb), v3(tc));
+}
+
 template <bool STATS>
 __device__ __forceinline__ void cw8_test_tri(const float4* tris, uint32_t k, const Ray& ray, Hit& h, Counters& cnt)
 {
     if (STATS) cnt.c[C_TRIS]++;
-    float4 ta, tb;
-    ldg256(tris + 4 * (size_t)k, ta, tb);
-    const float4 tc = __ldg(tris + 4 * (size_t)k + 2);
-    const float tt = tri_intersect(ray, v3(ta), v3(tb), v3(tc));
-    const uint32_t id = __float_as_uint(ta.w);
+    uint32_t id, slot;
+    const float tt = cw8_tri(tris, k, ray, id, slot);
     if (accept_strict(tt, id, h)) {
         h.t = tt;
         h.prim = id;
         h.kind = 1;
-        h.slot = __float_as_uint(tb.w);
+        h.slot = slot;
     }
+}
+
+// Position of the n-th (from 0) set bit of m, which has more than n.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n)
+{
+    for (; n != 0u; --n) m &= m - 1u;
+    return (uint32_t)(__ffs(m) - 1);
+}
+
+// The warp's remaining held primitives, shared out over all 32 lanes: item i
+// of the warp (lanes' items in lane order, each lane's in group and bit
+// order) is tested by lane i % 32 in step i / 32, with the owning lane's ray
+// and primitive array (a lane's own may be another scene's, or none) fetched
+// by shuffle.  Per step, the lanes that tested one owner's items form
+// a contiguous segment; a min-reduction over the segment picks its smallest
+// (distance, id) candidate with distance > EPSILON (positive floats order
+// like their bit patterns), and the owner takes it through accept_strict,
+// so the owner ends with the same hit as testing every item itself in any
+// order.  Every lane of the warp calls this (warp-synchronous).
+//   held: the calling lane's group entries (entry g at held[g * stride]),
+//   readable by the other lanes of the warp (shared memory, lane-adjacent);
+//   rest: the lane has items left: `cur` (its group in progress, taken from
+//   entry j - 1) and entries j .. nh - 1.
+template <bool STATS>
+__device__ __forceinline__ void cw8_warp_prims(const float4* tris, uint2* held, int stride, int lane, bool rest,
+                                               uint2 cur, int j, int nh, const Ray& ray, Hit& h, Counters& cnt)
+{
+    const unsigned full = 0xFFFFFFFFu;
+    int first = j;
+    uint32_t r = 0;
+    if (rest) {
+        if (cur.y != 0u) {
+            --first;  // j >= 1: cur came from entry j - 1
+            held[first * stride] = cur;
+        }
+        for (int g = first; g < nh; ++g) r += (uint32_t)__popc(held[g * stride].y);
+    }
+    __syncwarp();
+    uint32_t incl = r;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t excl = incl - r;
+    const uint32_t total = __shfl_sync(full, incl, 31);
+    for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t idx = base + (uint32_t)lane;
+        // owner: the last lane whose first item is at or before idx (it has
+        // items, as the next lane's first item is after idx)
+        int o = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t v = __shfl_sync(full, excl, o + step);
+            if (v <= idx) o += step;
+        }
+        const uint32_t eo = __shfl_sync(full, excl, o);
+        const uint32_t io = __shfl_sync(full, incl, o);
+        const int fo = __shfl_sync(full, first, o);
+        const Ray ro{V3{__shfl_sync(full, ray.o.x, o), __shfl_sync(full, ray.o.y, o), __shfl_sync(full, ray.o.z, o)},
+                     V3{__shfl_sync(full, ray.d.x, o), __shfl_sync(full, ray.d.y, o), __shfl_sync(full, ray.d.z, o)}};
+        const float4* to = reinterpret_cast<const float4*>(
+            __shfl_sync(full, static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(tris)), o));
+        uint32_t tk = 0xFFFFFFFFu, id = 0xFFFFFFFFu, slot = 0xFFFFFFFFu;
+        unsigned seg;
+        if (idx < total) {
+            uint32_t rank = idx - eo;
+            const uint2* hg = held + (o - lane);
+            int g = fo;
+            uint2 grp = hg[g * stride];
+            uint32_t c = (uint32_t)__popc(grp.y);
+            while (rank >= c) {
+                rank -= c;
+                ++g;
+                grp = hg[g * stride];
+                c = (uint32_t)__popc(grp.y);
+            }
+            if (STATS) cnt.c[C_TRIS]++;
+            uint32_t tid, tsl;
+            const float tt = cw8_tri(to, grp.x + nth_set_bit(grp.y, rank), ro, tid, tsl);
+            if (tt > EPSILON) {
+                tk = __float_as_uint(tt);
+                id = tid;
+                slot = tsl;
+            }
+            // this step's lanes holding the owner's items: [lo, hi)
+            const uint32_t lo = eo > base ? eo - base : 0u;
+            const uint32_t hi = io - base < 32u ? io - base : 32u;
+            seg = (hi == 32u ? full : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+        } else {
+            seg = full << (total - base);  // the idle lanes of the last step: total - base in [1, 31]
+        }
+        const uint32_t m1 = __reduce_min_sync(seg, tk);
+        const uint32_t m2 = __reduce_min_sync(seg, tk == m1 ? id : 0xFFFFFFFFu);
+        const uint32_t m3 = __reduce_min_sync(seg, (tk == m1 && id == m2) ? slot : 0xFFFFFFFFu);
+        // owners read their segment's result from its first lane
+        const bool mine = r != 0u && excl < base + 32u && incl > base;
+        const int src = mine ? (int)((excl > base ? excl : base) - base) : lane;
+        const uint32_t q1 = __shfl_sync(full, m1, src);
+        const uint32_t q2 = __shfl_sync(full, m2, src);
+        const uint32_t q3 = __shfl_sync(full, m3, src);
+        if (mine && q1 != 0xFFFFFFFFu && accept_strict(__uint_as_float(q1), q2, h)) {
+            h.t = __uint_as_float(q1);
+            h.prim = q2;
+            h.kind = 1;
+            h.slot = q3;
+        }
+    }
+    __syncwarp();
 }
 
 // Closest hit of one ray by one thread over the 8-wide BVH of a

@@ -353,8 +353,18 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
 
 // Primitive groups a lane of the 8-wide traversal may hold back while the
 // warp's slowest lane is still looking for its first (c1 frame, ms: 1 ->
-// 100.8, 2 -> 69.1, 4 -> 61.1, 6 -> 60.9, 8 -> 61.1, 12 -> 63.1).
+// 100.8, 2 -> 69.1, 4 -> 61.1, 6 -> 60.9, 8 -> 61.1, 12 -> 63.1; with the
+// shared primitive phase below: 4 -> 61.4, 5 -> 60.6, 6 -> 60.4).  Capping
+// the primitives held instead (12, 16, 20) measured 61.3-63.1.
 constexpr int kCw8Postpone = 6;
+
+// Held primitives are tested one per lane and step while at least this many
+// lanes of the warp have some left; the rest are shared out over all 32
+// lanes (cw8_warp_prims).  1 = never shared.  c1 frame, ms: 1 -> 61.4,
+// 4 -> 61.2, 6 -> 60.6, 8 -> 60.1-60.4, 10 -> 60.6, 12 -> 60.8, 16 -> 62.1,
+// 20 -> 64.1, 26 -> 68.7: a shared step costs several sequential ones (the
+// owner search, the ray and result shuffles), so only the tail is shared.
+constexpr int kCw8SharedBelow = 8;
 
 // The extend kernel over the compressed 8-wide BVH (triangle scenes; strict
 // ties).  Same phases as wf_extend_bvh: idle lanes fetch rays; all lanes visit
@@ -365,6 +375,9 @@ constexpr int kCw8Postpone = 6;
 // all lanes test their held primitives, one per lane and step.  Node groups
 // are visited nearest-octant first; which boxes are entered depends on the
 // order, the closest hit under strict ties does not.
+// 64 registers, eight 128-thread blocks per SM; bounds for 10 or 12 blocks
+// (48 or 40 registers) spill 190 / 298 bytes and measured 65.7 / 75.0 ms on
+// the c1 frame against 60.4.
 template <bool STATS, bool MULTI, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     wf_extend_cw8(TraceArgs a, WfState s, int qsel, const TraceArgs* slots)
@@ -472,13 +485,15 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                 }
             }
         }
-        // 3) the held primitives, one per lane and step
+        // 3) the held primitives: one per lane and step while at least
+        // kCw8SharedBelow lanes have some left, then the rest shared out
+        // over the warp
         {
             int j = 0;
             uint2 cur = make_uint2(0u, 0u);
             for (;;) {
                 const bool lf = has && (cur.y != 0u || j < nh);
-                if (!__any_sync(full, lf)) break;
+                if (__popc(__ballot_sync(full, lf)) < kCw8SharedBelow) break;
                 if (lf) {
                     if (cur.y == 0u) {
                         cur = held[j * BLOCK];
@@ -489,6 +504,8 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                     cw8_test_tri<STATS>(tris, cur.x + (uint32_t)bit, ray, h, cnt);
                 }
             }
+            const bool rest = has && (cur.y != 0u || j < nh);
+            if (__any_sync(full, rest)) cw8_warp_prims<STATS>(tris, held, BLOCK, lane, rest, cur, j, nh, ray, h, cnt);
         }
         nh = 0;
         // 4) finished rays: planes and the result
@@ -723,6 +740,14 @@ static cudaError_t extend_bvh_b(const TraceArgs& a, const WfState& s, const WfCo
     auto k = c.wide == WF_WIDTH_8   ? wf_extend_cw8<STATS, MULTI, BLOCK>
              : c.wide == WF_WIDTH_4 ? wf_extend_bvh<TIE, STATS, MULTI, BLOCK, true>
                                     : wf_extend_bvh<TIE, STATS, MULTI, BLOCK, false>;
+    if (c.wide == WF_WIDTH_8 && c.cw8_stack != 0) {
+        TraceArgs a8 = a;
+        a8.stack_depth = c.cw8_stack;
+        const size_t smem = wf_extend_smem(a8.stack_depth, BLOCK, c.wide);
+        smem_attr(k, smem);
+        k<<<c.extend_grid, BLOCK, smem, st>>>(a8, s, qsel, c.slots);
+        return cudaGetLastError();
+    }
     const size_t smem = wf_extend_smem(a.stack_depth, BLOCK, c.wide);
     smem_attr(k, smem);
     k<<<c.extend_grid, BLOCK, smem, st>>>(a, s, qsel, c.slots);
@@ -859,6 +884,7 @@ static int occ_bvh(uint32_t block, size_t stack_depth, int wide)
 int wf_extend_blocks_per_sm(const WfConfig& c, uint32_t stack_depth)
 {
     const int w = c.wide;
+    if (w == WF_WIDTH_8 && c.cw8_stack != 0) stack_depth = c.cw8_stack;
     if (c.multi) return c.stats ? occ_bvh<TIE_STRICT, true, true>(c.block, stack_depth, w)
                                 : occ_bvh<TIE_STRICT, false, true>(c.block, stack_depth, w);
     if (c.bvh) return c.stats ? occ_bvh<TIE_STRICT, true, false>(c.block, stack_depth, w)

@@ -32,6 +32,8 @@ struct WfConfig {
     int multi;                // batched: per-slot scene table
     int has_emitters;         // some scene has emissive spheres (shade needs a traversal stack)
     int wide;                 // extend's BVH: WF_WIDTH_2 (binary), WF_WIDTH_4 or WF_WIDTH_8 (every scene has it)
+    uint32_t cw8_stack;       // WF_WIDTH_8: the extend kernel's stack entries (the 8-wide depth; 0 = the
+                              // launch's stack_depth, which the shade and finishing kernels use)
     uint32_t block;           // extend kernel threads per block: 64, 128 or 256
     uint32_t extend_grid, shade_grid;
     uint32_t finish_grid;     // blocks of 128 threads of the finishing kernel
