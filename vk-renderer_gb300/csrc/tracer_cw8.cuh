@@ -137,6 +137,35 @@ __device__ __forceinline__ void cw8_test_tri(const float4* tris, uint32_t k, con
     }
 }
 
+// Tests primitives k0 and, if two, k1: both records are fetched before
+// either test, so the two L2 round trips overlap.
+template <bool STATS>
+__device__ __forceinline__ void cw8_test_tri2(const float4* tris, uint32_t k0, uint32_t k1, bool two, const Ray& ray,
+                                              Hit& h, Counters& cnt)
+{
+    if (STATS) cnt.c[C_TRIS] += two ? 2 : 1;
+    float4 a0, b0, a1, b1;
+    ldg256(tris + 4 * (size_t)k0, a0, b0);
+    const float4 c0 = __ldg(tris + 4 * (size_t)k0 + 2);
+    const uint32_t k = two ? k1 : k0;
+    ldg256(tris + 4 * (size_t)k, a1, b1);
+    const float4 c1 = __ldg(tris + 4 * (size_t)k + 2);
+    const float t0 = tri_intersect(ray, v3(a0), v3(b0), v3(c0));
+    const float t1 = tri_intersect(ray, v3(a1), v3(b1), v3(c1));
+    if (accept_strict(t0, __float_as_uint(a0.w), h)) {
+        h.t = t0;
+        h.prim = __float_as_uint(a0.w);
+        h.kind = 1;
+        h.slot = __float_as_uint(b0.w);
+    }
+    if (two && accept_strict(t1, __float_as_uint(a1.w), h)) {
+        h.t = t1;
+        h.prim = __float_as_uint(a1.w);
+        h.kind = 1;
+        h.slot = __float_as_uint(b1.w);
+    }
+}
+
 // Position of the n-th (from 0) set bit of m, which has more than n.
 __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n)
 {
@@ -144,23 +173,62 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n)
     return (uint32_t)(__ffs(m) - 1);
 }
 
+// Per-lane record of the shared primitive phase, in shared memory: what the
+// other lanes of the warp need to test this lane's primitives for it.
+struct alignas(16) Cw8Share {
+    float4 o, d;               // the ray
+    unsigned long long best;   // (distance bits << 32) | id of the best hit so far
+    const float4* tris;        // the lane's scene's primitives (8-wide order)
+    uint32_t excl, first;      // the lane's first item in the warp's order, its first group entry
+    uint32_t slot, pad;        // storage slot of the hit that set `best`
+};
+static_assert(sizeof(Cw8Share) == 64, "shared record is 64 bytes");
+
+// (distance, id) as one integer that orders like the strict (t, id) order
+// for non-negative distances (their bit patterns order like their values).
+__device__ __forceinline__ unsigned long long hit_key(float t, uint32_t id)
+{
+    return ((unsigned long long)__float_as_uint(t) << 32) | id;
+}
+
+// Position of the n-th (from 0) set bit of m, which has more than n: popc
+// bisection, a fixed number of steps.
+__device__ __forceinline__ uint32_t nth_bit32(uint32_t m, uint32_t n)
+{
+    uint32_t pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 2; w >>= 1) {
+        const uint32_t c = (uint32_t)__popc(m & ((1u << w) - 1u));
+        if (n >= c) {
+            n -= c;
+            pos += (uint32_t)w;
+            m >>= w;
+        }
+    }
+    return pos + ((n >= (m & 1u)) ? 1u : 0u);
+}
+
 // The warp's remaining held primitives, shared out over all 32 lanes: item i
 // of the warp (lanes' items in lane order, each lane's in group and bit
-// order) is tested by lane i % 32 in step i / 32, with the owning lane's ray
-// and primitive array (a lane's own may be another scene's, or none) fetched
-// by shuffle.  Per step, the lanes that tested one owner's items form
-// a contiguous segment; a min-reduction over the segment picks its smallest
-// (distance, id) candidate with distance > EPSILON (positive floats order
-// like their bit patterns), and the owner takes it through accept_strict,
-// so the owner ends with the same hit as testing every item itself in any
-// order.  Every lane of the warp calls this (warp-synchronous).
+// order) is tested by lane i % 32 in step i / 32.  Each lane with items
+// publishes its ray, primitive array, best hit and item offset in its
+// Cw8Share record; a step's lanes find their owners from a ballot of the
+// owners with items in the step and the step's segment starts, fetch the
+// owner's ray from its record, and lower the owner's best (distance, id) key
+// with a shared-memory atomic minimum (a candidate counts when distance >
+// EPSILON; min over the keys is the strict-ties order, so the owner ends with
+// the hit it would get testing every item itself, in any order); the lane
+// whose candidate is the minimum after the step records its slot.  Every
+// lane of the warp calls this (warp-synchronous).
 //   held: the calling lane's group entries (entry g at held[g * stride]),
-//   readable by the other lanes of the warp (shared memory, lane-adjacent);
-//   rest: the lane has items left: `cur` (its group in progress, taken from
-//   entry j - 1) and entries j .. nh - 1.
+//   readable by the other lanes of the warp; sh: the calling lane's record
+//   (the warp's lanes' records adjacent); rest: the lane has items left:
+//   `cur` (its group in progress, taken from entry j - 1) and entries
+//   j .. nh - 1.
 template <bool STATS>
-__device__ __forceinline__ void cw8_warp_prims(const float4* tris, uint2* held, int stride, int lane, bool rest,
-                                               uint2 cur, int j, int nh, const Ray& ray, Hit& h, Counters& cnt)
+__device__ __forceinline__ void cw8_warp_prims(const float4* tris, uint2* held, Cw8Share* sh, int stride, int lane,
+                                               bool rest, uint2 cur, int j, int nh, const Ray& ray, Hit& h,
+                                               Counters& cnt)
 {
     const unsigned full = 0xFFFFFFFFu;
     int first = j;
@@ -172,7 +240,6 @@ __device__ __forceinline__ void cw8_warp_prims(const float4* tris, uint2* held, 
         }
         for (int g = first; g < nh; ++g) r += (uint32_t)__popc(held[g * stride].y);
     }
-    __syncwarp();
     uint32_t incl = r;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -181,29 +248,36 @@ __device__ __forceinline__ void cw8_warp_prims(const float4* tris, uint2* held, 
     }
     const uint32_t excl = incl - r;
     const uint32_t total = __shfl_sync(full, incl, 31);
+    const unsigned long long key0 = hit_key(h.t, h.prim);
+    if (rest) {
+        sh->o = make_float4(ray.o.x, ray.o.y, ray.o.z, 0.0f);
+        sh->d = make_float4(ray.d.x, ray.d.y, ray.d.z, 0.0f);
+        sh->best = key0;
+        sh->tris = tris;
+        sh->excl = excl;
+        sh->first = (uint32_t)first;
+    }
+    __syncwarp();
+    Cw8Share* const wsh = sh - lane;
     for (uint32_t base = 0; base < total; base += 32u) {
         const uint32_t idx = base + (uint32_t)lane;
-        // owner: the last lane whose first item is at or before idx (it has
-        // items, as the next lane's first item is after idx)
-        int o = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-            const uint32_t v = __shfl_sync(full, excl, o + step);
-            if (v <= idx) o += step;
-        }
-        const uint32_t eo = __shfl_sync(full, excl, o);
-        const uint32_t io = __shfl_sync(full, incl, o);
-        const int fo = __shfl_sync(full, first, o);
-        const Ray ro{V3{__shfl_sync(full, ray.o.x, o), __shfl_sync(full, ray.o.y, o), __shfl_sync(full, ray.o.z, o)},
-                     V3{__shfl_sync(full, ray.d.x, o), __shfl_sync(full, ray.d.y, o), __shfl_sync(full, ray.d.z, o)}};
-        const float4* to = reinterpret_cast<const float4*>(
-            __shfl_sync(full, static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(tris)), o));
-        uint32_t tk = 0xFFFFFFFFu, id = 0xFFFFFFFFu, slot = 0xFFFFFFFFu;
-        unsigned seg;
+        // owners with items in this step, in lane order = the step's segments
+        const unsigned in = __ballot_sync(full, r != 0u && excl < base + 32u && incl > base);
+        const unsigned starts =
+            __reduce_or_sync(full, (r != 0u && excl >= base && excl < base + 32u) ? 1u << (excl - base) : 0u);
+        unsigned long long key = ~0ull;
+        Cw8Share* osh = wsh;
+        uint32_t slot = 0;
         if (idx < total) {
-            uint32_t rank = idx - eo;
+            // segment of this lane: starts at or before it, plus one if the
+            // step opens inside an earlier owner's items
+            const unsigned upto = lane == 31 ? starts : (starts & ((2u << lane) - 1u));
+            const uint32_t n = (uint32_t)__popc(upto) - 1u + ((starts & 1u) ? 0u : 1u);
+            const int o = (int)nth_bit32(in, n);
+            osh = wsh + o;
+            uint32_t rank = idx - osh->excl;
             const uint2* hg = held + (o - lane);
-            int g = fo;
+            int g = (int)osh->first;
             uint2 grp = hg[g * stride];
             uint32_t c = (uint32_t)__popc(grp.y);
             while (rank >= c) {
@@ -213,34 +287,25 @@ __device__ __forceinline__ void cw8_warp_prims(const float4* tris, uint2* held, 
                 c = (uint32_t)__popc(grp.y);
             }
             if (STATS) cnt.c[C_TRIS]++;
-            uint32_t tid, tsl;
-            const float tt = cw8_tri(to, grp.x + nth_set_bit(grp.y, rank), ro, tid, tsl);
+            const Ray ro{v3(osh->o), v3(osh->d)};
+            uint32_t tid;
+            const float tt = cw8_tri(osh->tris, grp.x + nth_set_bit(grp.y, rank), ro, tid, slot);
             if (tt > EPSILON) {
-                tk = __float_as_uint(tt);
-                id = tid;
-                slot = tsl;
+                key = hit_key(tt, tid);
+                atomicMin(&osh->best, key);
             }
-            // this step's lanes holding the owner's items: [lo, hi)
-            const uint32_t lo = eo > base ? eo - base : 0u;
-            const uint32_t hi = io - base < 32u ? io - base : 32u;
-            seg = (hi == 32u ? full : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-        } else {
-            seg = full << (total - base);  // the idle lanes of the last step: total - base in [1, 31]
         }
-        const uint32_t m1 = __reduce_min_sync(seg, tk);
-        const uint32_t m2 = __reduce_min_sync(seg, tk == m1 ? id : 0xFFFFFFFFu);
-        const uint32_t m3 = __reduce_min_sync(seg, (tk == m1 && id == m2) ? slot : 0xFFFFFFFFu);
-        // owners read their segment's result from its first lane
-        const bool mine = r != 0u && excl < base + 32u && incl > base;
-        const int src = mine ? (int)((excl > base ? excl : base) - base) : lane;
-        const uint32_t q1 = __shfl_sync(full, m1, src);
-        const uint32_t q2 = __shfl_sync(full, m2, src);
-        const uint32_t q3 = __shfl_sync(full, m3, src);
-        if (mine && q1 != 0xFFFFFFFFu && accept_strict(__uint_as_float(q1), q2, h)) {
-            h.t = __uint_as_float(q1);
-            h.prim = q2;
+        __syncwarp();
+        if (key != ~0ull && key == *reinterpret_cast<volatile unsigned long long*>(&osh->best)) osh->slot = slot;
+        __syncwarp();
+    }
+    if (rest) {
+        const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&sh->best);
+        if (k != key0) {
+            h.t = __uint_as_float((uint32_t)(k >> 32));
+            h.prim = (uint32_t)k;
             h.kind = 1;
-            h.slot = q3;
+            h.slot = *reinterpret_cast<volatile uint32_t*>(&sh->slot);
         }
     }
     __syncwarp();

@@ -358,13 +358,15 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
 // the primitives held instead (12, 16, 20) measured 61.3-63.1.
 constexpr int kCw8Postpone = 6;
 
-// Held primitives are tested one per lane and step while at least this many
+// Held primitives are tested two per lane and step while at least this many
 // lanes of the warp have some left; the rest are shared out over all 32
-// lanes (cw8_warp_prims).  1 = never shared.  c1 frame, ms: 1 -> 61.4,
-// 4 -> 61.2, 6 -> 60.6, 8 -> 60.1-60.4, 10 -> 60.6, 12 -> 60.8, 16 -> 62.1,
-// 20 -> 64.1, 26 -> 68.7: a shared step costs several sequential ones (the
-// owner search, the ray and result shuffles), so only the tail is shared.
-constexpr int kCw8SharedBelow = 8;
+// lanes (cw8_warp_prims).  1 = never shared, 33 = always.  c1 frame, ms:
+// 1 -> 60.4, 8 -> 58.1, 12 -> 58.0, 16 -> 58.4, 24 -> 61.3, 33 -> 67.8: a
+// shared step (owner look-up, the owner's ray from shared memory, an atomic
+// minimum) takes longer than a sequential one, so only the tail is shared.
+// (One primitive per sequential step and the owner found by shuffles
+// instead: 61.4 unshared, 60.1-60.4 at 8.)
+constexpr int kCw8SharedBelow = 12;
 
 // The extend kernel over the compressed 8-wide BVH (triangle scenes; strict
 // ties).  Same phases as wf_extend_bvh: idle lanes fetch rays; all lanes visit
@@ -372,9 +374,10 @@ constexpr int kCw8SharedBelow = 8;
 // interior children become a node group on the stack, the hit leaves a
 // primitive group held back) until every lane still tracing holds some
 // primitives, lanes that hold fewer than kCw8Postpone groups going on; then
-// all lanes test their held primitives, one per lane and step.  Node groups
-// are visited nearest-octant first; which boxes are entered depends on the
-// order, the closest hit under strict ties does not.
+// all lanes test their held primitives, two per lane and step (both records
+// fetched before either test), the warp sharing out the last ones.  Node
+// groups are visited nearest-octant first; which boxes are entered depends
+// on the order, the closest hit under strict ties does not.
 // 64 registers, eight 128-thread blocks per SM; bounds for 10 or 12 blocks
 // (48 or 40 registers) spill 190 / 298 bytes and measured 65.7 / 75.0 ms on
 // the c1 frame against 60.4.
@@ -385,10 +388,13 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     extern __shared__ int smem[];
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
-    // stack of node groups, then held primitive groups; entry j of a thread
-    // at j * BLOCK + threadIdx.x
+    // stack of node groups, then held primitive groups (entry j of a thread
+    // at j * BLOCK + threadIdx.x), then the threads' shared-phase records
     uint2* stk = reinterpret_cast<uint2*>(smem) + threadIdx.x;
     uint2* held = reinterpret_cast<uint2*>(smem) + (size_t)a.stack_depth * BLOCK + threadIdx.x;
+    Cw8Share* shr =
+        reinterpret_cast<Cw8Share*>(reinterpret_cast<uint2*>(smem) + ((size_t)a.stack_depth + kCw8Postpone) * BLOCK) +
+        threadIdx.x;
     const int cap = (int)a.stack_depth;
     const uint32_t total = s.count[qsel];
     const uint32_t* queue = qsel ? s.queue[1] : s.queue[0];
@@ -485,7 +491,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                 }
             }
         }
-        // 3) the held primitives: one per lane and step while at least
+        // 3) the held primitives: two per lane and step while at least
         // kCw8SharedBelow lanes have some left, then the rest shared out
         // over the warp
         {
@@ -499,13 +505,20 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
                         cur = held[j * BLOCK];
                         ++j;
                     }
-                    const int bit = __ffs(cur.y) - 1;
+                    const uint32_t k0 = cur.x + (uint32_t)(__ffs(cur.y) - 1);
                     cur.y &= cur.y - 1u;
-                    cw8_test_tri<STATS>(tris, cur.x + (uint32_t)bit, ray, h, cnt);
+                    if (cur.y == 0u && j < nh) {
+                        cur = held[j * BLOCK];
+                        ++j;
+                    }
+                    const bool two = cur.y != 0u;
+                    const uint32_t k1 = two ? cur.x + (uint32_t)(__ffs(cur.y) - 1) : k0;
+                    if (two) cur.y &= cur.y - 1u;
+                    cw8_test_tri2<STATS>(tris, k0, k1, two, ray, h, cnt);
                 }
             }
             const bool rest = has && (cur.y != 0u || j < nh);
-            if (__any_sync(full, rest)) cw8_warp_prims<STATS>(tris, held, BLOCK, lane, rest, cur, j, nh, ray, h, cnt);
+            if (__any_sync(full, rest)) cw8_warp_prims<STATS>(tris, held, shr, BLOCK, lane, rest, cur, j, nh, ray, h, cnt);
         }
         nh = 0;
         // 4) finished rays: planes and the result
@@ -731,7 +744,7 @@ static void smem_attr(K k, size_t smem)
 // reference) or held primitive groups (8-wide: 8 B per group).
 static size_t wf_extend_smem(size_t stack_depth, uint32_t block, int wide)
 {
-    return (stack_depth * 8 + (wide == WF_WIDTH_8 ? kCw8Postpone * 8 : kPostpone * 4)) * block;
+    return (stack_depth * 8 + (wide == WF_WIDTH_8 ? kCw8Postpone * 8 + sizeof(Cw8Share) : kPostpone * 4)) * block;
 }
 
 template <int TIE, bool STATS, bool MULTI, int BLOCK>
