@@ -39,10 +39,12 @@ UNIT = "Mrays/s"
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ray of the
-# extend kernel, from one ncu capture of every extend launch of the c1 scene
-# at 640x360x4 spp (profiles/wf_extend_bvh_c1_small.md); traffic grows with
-# the number of rays, so the frame's traffic is this times its rays.
-NCU_EXTEND_DRAM_BYTES_PER_RAY = 113.1
+# 8-wide extend kernel, from one ncu capture of every extend launch of two
+# whole c1 frames (1920x1080, 16 spp, finishing kernel off so that every ray
+# goes through it: 3.816 GB read + 0.26 GB written per frame of 67.6 M rays;
+# profiles/wf_extend_cw8_c1_dram.md); the frame's traffic is this times its
+# rays.
+NCU_EXTEND_DRAM_BYTES_PER_RAY = 60.3
 
 
 def peaks():
