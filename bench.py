@@ -411,12 +411,14 @@ def adjoint_section(local: int, steps: int) -> dict:
                                    outputs=(ga.data_ptr(), ge.data_ptr(), gc.data_ptr()), stream=sptr)
     ms_adj = timed(adj)  # AUTO: the wavefront (c3 has no emissive spheres)
     adj_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
-    # both adjoint forms on the same inputs, for comparison
+    # both adjoint forms on the same inputs, for comparison: forward rays per
+    # second of each, and the rays each traced
     per_kernel = {}
     for name, k in (("per_pixel", abi.KERNEL_PLAIN), ("wavefront", abi.KERNEL_WAVEFRONT)):
         p_run.kernel = k
         ms_k = timed(adj)
-        per_kernel[name] = {"value": adj_rays / (ms_k / 1e3) / 1e6, "ms_per_step": ms_k}
+        k_rays = sum(tr.stats()[q] for q in ("closest_rays", "shadow_rays"))
+        per_kernel[name] = {"value": fwd_rays / (ms_k / 1e3) / 1e6, "ms_per_step": ms_k, "traced_rays": k_rays}
     p_run.kernel = abi.KERNEL_AUTO
     g_alb = ga.cpu().numpy().astype(np.float64)
     # spot check: central differences, step 1e-3, on the 6 largest components.
@@ -452,16 +454,18 @@ def adjoint_section(local: int, steps: int) -> dict:
     tr.close()
     fwd = fwd_rays / (ms_fwd / 1e3) / 1e6
     # headline: the forward frame's rays per second of adjoint time, i.e.
-    # adjoint speed against forward speed on the same frame (the replay traces
-    # every ray twice; that count is reported beside it)
+    # adjoint speed against forward speed on the same frame; beside it the
+    # rays the adjoint traced (pass 1 once more, and pass 2 too unless it
+    # replays pass 1's logged hits)
     adjv = fwd_rays / (ms_adj / 1e3) / 1e6
     replay = adj_rays / (ms_adj / 1e3) / 1e6
     return {"metric": "adjoint Mrays/s (c3, path replay; forward rays per adjoint second)", "value": adjv,
             "unit": UNIT, "ms_per_step": ms_adj,
             "forward": {"value": fwd, "ms_per_step": ms_fwd, "rays_per_step": fwd_rays},
             "ratio_adjoint_to_forward": ms_fwd / ms_adj,
-            "replay_rays": {"rays_per_step": adj_rays, "mrays_per_s": replay,
-                            "ratio_to_forward_mrays_per_s": replay / fwd},
+            "traced_rays": {"rays_per_step": adj_rays, "mrays_per_s": replay,
+                            "ratio_to_forward_mrays_per_s": replay / fwd,
+                            "pass2_from_hit_log": bool(adj_rays < 2 * fwd_rays)},
             "kernel": "auto (wavefront: no emissive spheres)",
             "kernels": per_kernel,
             "grad_check": {"max_rel_err_vs_central_fd": max(rel), "step": 1e-3,
@@ -810,7 +814,7 @@ def gd_section(local: int, gd_steps: int, width: int, spp: int, n_tris: int, che
     err1 = np.abs(opt.albedo - truth["albedo"])[seen]
     return {"metric": "gradient descent on albedos (c4 shape)", "steps": gd_steps, "resumed_at_step": first,
             "forward_mrays_s": {"median": float(np.median(fwd_rates)), "min": float(np.min(fwd_rates))},
-            # forward rays per adjoint second (the replay traces each ray twice)
+            # forward rays per adjoint second
             "adjoint_mrays_s": {"median": float(np.median(adj_rates)), "min": float(np.min(adj_rates))},
             "adjoint_to_forward": float(np.median(adj_rates) / np.median(fwd_rates)),
             "albedo_mae": {"initial": float(err0.mean()), "final": float(err1.mean()),

@@ -271,9 +271,14 @@ int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* byt
  * NULL): d_albedo and d_emission num_materials*3 floats, d_campos 3 floats.
  * Each pointer may be host or device memory; with host outputs the call
  * waits (bounded) for the result, with device outputs it is asynchronous on
- * cuda_stream.  Path replay: every sample is traced twice more (no path
- * vertices are stored); the Russian-roulette normalisation is treated as a
- * constant.  Materials of spheres and planes (stored inline) get no gradient.
+ * cuda_stream.  Path replay: every sample is traced again (pass 1, giving
+ * its radiance) and then replayed with the gradient terms (pass 2, the same
+ * rays): the per-pixel form traces pass 2's rays too; the wavefront form
+ * (scenes without emissive spheres) keeps pass 1's closest hits of each
+ * pixel's current sample (16 bytes x max_depth per pixel, within the limit
+ * tracer_set_adjoint_hit_log sets; beyond it pass 2 traces) and pass 2 reads
+ * them instead of tracing.  The Russian-roulette normalisation is treated as
+ * a constant.  Materials of spheres and planes (stored inline) get no gradient.
  * d_campos is the interior part (the camera position enters next-event
  * shading through the view vector and the hit points: the derivative of the
  * point-sampled image away from outlines, zero for scenes without emissive
@@ -296,6 +301,15 @@ int tracer_trace_adjoint(tracer_ctx* ctx, const tracer_frame* frame, const trace
  * default.  At most 1024.  Applies to every later adjoint of the context.
  * No counterpart in the reference. */
 int tracer_set_edge_sampling(tracer_ctx* ctx, uint32_t samples_per_edge);
+
+/* Device memory the wavefront adjoint may keep pass 1's closest hits in
+ * (width x height x max_depth x 16 bytes; allocated on first use and kept
+ * for later adjoints of the context): pass 2 then replays them without
+ * tracing, which halves the adjoint's traced rays with the same gradients.
+ * A trace whose hits would exceed the limit traces pass 2 instead.  0 = never
+ * keep them (frees the buffer); default 4 GiB.  No counterpart in the
+ * reference. */
+int tracer_set_adjoint_hit_log(tracer_ctx* ctx, uint64_t max_bytes);
 
 /* ------------------------------------------------------------ batches
  * Many independent scenes of uneven size and resolution traced together (no

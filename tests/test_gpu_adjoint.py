@@ -143,13 +143,18 @@ def test_adjoint_vs_fp64_host(gpu_tracer):
     _compare(ga, fd, "albedo vs FP64")
 
 
+@pytest.mark.parametrize("hit_log", [True, False])
 @pytest.mark.parametrize("case", ["sah-rr0", "sah-rr3-ragged", "linear-reference-ties"])
-def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case):
-    """Scenes without emitters take the wavefront adjoint (both passes as
-    queue stages, closest hits through the forward extend kernel); the
-    per-pixel adjoint kernel runs the same passes.  Ray and hit counts are
-    equal; gradients are equal up to the order of the FP64 sums."""
+def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case, hit_log):
+    """Scenes without emitters take the wavefront adjoint (closest hits
+    through the forward extend kernel); the per-pixel adjoint kernel traces
+    both passes of every sample.  With the hit log (the default) the
+    wavefront traces pass 1 only and replays pass 2 from the logged hits:
+    exactly half the per-pixel kernel's rays and hits; without it (limit 0)
+    it traces both passes: the same counts.  Gradients are equal up to the
+    order of the FP64 sums either way."""
     tr = gpu_tracer
+    tr.set_adjoint_hit_log((4 << 30) if hit_log else 0)
     sc = _scene(seed=21, n=2000, nm=16)
     tie = abi.TIES_STRICT
     if case.startswith("linear"):
@@ -180,13 +185,17 @@ def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case):
     pa, pe, pc, ps = out[(abi.KERNEL_PLAIN, 0)]
     for key in ((abi.KERNEL_WAVEFRONT, 1), (abi.KERNEL_WAVEFRONT, 0xFFFFFFFF), (abi.KERNEL_WAVEFRONT, 700)):
         wa, we, wc, ws = out[key]
-        assert ps["closest_rays"] == ws["closest_rays"] and ps["hits"] == ws["hits"], key
+        if hit_log:
+            assert ps["closest_rays"] == 2 * ws["closest_rays"] and ps["hits"] == 2 * ws["hits"], key
+        else:
+            assert ps["closest_rays"] == ws["closest_rays"] and ps["hits"] == ws["hits"], key
         assert ps["shadow_rays"] == ws["shadow_rays"] == 0
         assert np.all(wc == 0.0) and np.all(pc == 0.0)
         for a, b in ((pa, wa), (pe, we)):
             scale = float(np.max(np.abs(a))) if np.any(a) else 1.0
             np.testing.assert_allclose(b, a, rtol=1e-5, atol=1e-7 * scale, err_msg=str(key))
         assert np.any(wa != 0)
+    tr.set_adjoint_hit_log(4 << 30)
 
 
 def _nee_scene(kind):

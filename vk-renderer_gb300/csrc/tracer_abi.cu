@@ -86,8 +86,10 @@ struct AdjBuffers {
     DevBuf<double> grad;  // FP64 sums the kernel accumulates into
     DevBuf<float> gradf;  // the same, rounded to float for the outputs
     DevBuf<float4> pix;   // wavefront form: per-pixel delta and sample-start RNG state
+    DevBuf<uint4> log;    // wavefront form: pass 1's closest hits of the current sample, per pixel
     void release()
     {
+        log.release();
         pix.release();
         dldi.release();
         lin.release();
@@ -166,6 +168,7 @@ struct tracer_ctx {
     DevBuf<unsigned char> pres_src[2], pres_out;  // staging for host images
     uint32_t trav_cap = 0;            // tracer_set_traversal_limit: 0 = automatic
     uint32_t edge_samples = 0;        // tracer_set_edge_sampling: pieces per triangle edge, 0 = off
+    uint64_t adj_log_limit = 4ull << 30;  // tracer_set_adjoint_hit_log: bytes for pass 1's hits, 0 = none
 };
 
 namespace {
@@ -625,6 +628,14 @@ int tracer_set_traversal_limit(tracer_ctx* c, uint32_t steps)
     int r = finish(c);
     if (r != TRACER_OK) return r;
     c->trav_cap = steps;
+    return TRACER_OK;
+}
+
+int tracer_set_adjoint_hit_log(tracer_ctx* c, uint64_t max_bytes)
+{
+    if (!c) return TRACER_ERR_INVALID_ARG;
+    c->adj_log_limit = max_bytes;
+    if (max_bytes == 0) c->adj.log.release();
     return TRACER_OK;
 }
 
@@ -1812,6 +1823,10 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     if (use_wf) {
         e = ensure_wavefront(c, npx);
         if (e == cudaSuccess) e = dalloc(ab.pix, npx);
+        // pass 1's hits for pass 2 to replay without tracing, when they fit the limit
+        const size_t log_n = npx * (size_t)p->max_depth;
+        const bool use_log = log_n * sizeof(uint4) <= c->adj_log_limit;
+        if (e == cudaSuccess && use_log) e = dalloc(ab.log, log_n);
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront adjoint state allocation");
         a.pixel_base = 0;
         a.num_slots = (uint32_t)npx;
@@ -1827,7 +1842,7 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         a.stack_depth = wstack;
         if (wc.wide == WF_WIDTH_8) wc.cw8_stack = s.cw8_depth;
         if (wc.wide != WF_WIDTH_8) a.sc.tri_cw8 = a.sc.tri_cw8_prims = nullptr;
-        const AdjWf aw{dldi, lin, ab.grad.p, s.nm, ab.pix.p};
+        const AdjWf aw{dldi, lin, ab.grad.p, s.nm, ab.pix.p, use_log ? ab.log.p : nullptr};
         c->last_kernel = TRACER_KERNEL_WAVEFRONT;
         c->last_launches = 1;  // + generate, rounds; the FP64-to-float conversion
         if (c->profiling) cudaEventRecord(c->prof_begin, st);

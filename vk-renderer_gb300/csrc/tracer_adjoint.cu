@@ -521,42 +521,17 @@ __device__ __forceinline__ void adj_store(const WfState& s, uint32_t pid, const 
                                __uint_as_float((p.replay ? kPhaseReplay : 0u) | (p.sample << 16) | p.depth));
 }
 
-// One bounce of whichever pass the path is in, given the closest hit h of
-// its ray, then the bookkeeping: pass 1 ends -> pass 2 of the same sample
-// from the sample's first ray and RNG state; pass 2 ends -> the next sample
-// (the RNG continues where pass 1 left it).  pix: the pixel's delta and the
-// RNG salt at the sample's start; prim0: the salt at the end of pass 1.
-// Returns true while the pixel has a ray to trace.
+// Pass 2's bounce at p.depth, given the closest hit h of its ray (the same
+// ray and hit as pass 1's bounce at that depth): the gradient terms, then
+// the same scatter and roulette as pass 1.  Returns true while the sample's
+// path goes on.
 template <class TR>
-__device__ __forceinline__ bool adj_advance(TR& tr, const TraceArgs& a, const AdjWf& w, uint32_t x, uint32_t y,
-                                            const Hit& h, AdjPath& p, float4* pix, uint32_t* prim0)
+__device__ __forceinline__ bool adj_replay_bounce(TR& tr, const TraceArgs& a, const AdjWf& w, const Hit& h, V3 delta,
+                                                  AdjPath& p)
 {
     double* gal = w.grad;
     double* gem = w.grad + 3 * (size_t)w.nm;
     const bool found = h.kind != 0;
-    if (!p.replay) {
-        // pass 1: clamp bookkeeping, then the forward bounce
-        if (p.acc.x < 0.0f || p.acc.x > 1.0f) { p.lc[0] = (int)p.depth; p.T.x = 0.0f; }
-        if (p.acc.y < 0.0f || p.acc.y > 1.0f) { p.lc[1] = (int)p.depth; p.T.y = 0.0f; }
-        if (p.acc.z < 0.0f || p.acc.z > 1.0f) { p.lc[2] = (int)p.depth; p.T.z = 0.0f; }
-        p.acc = vclamp01(p.acc);
-        const V3 before = p.acc;
-        const bool cont = shade_bounce<false>(tr, a, p.depth, found, h, p.ray, p.acc, p.mask, p.g);  // no emitters
-        p.T = p.T + (p.acc - before);
-        p.depth++;
-        if (cont && p.depth < a.max_depth) return true;
-        // pass 2 of the same sample: its first ray and RNG state again
-        *prim0 = __float_as_uint(p.g.salt);
-        p.g.salt = pix->w;
-        p.ray = primary_ray(a, x, y);
-        p.acc = splat(0.0f);
-        p.mask = splat(1.0f);
-        p.depth = 0;
-        p.replay = true;
-        return true;
-    }
-    // pass 2: the same bounce, with its gradient terms
-    const V3 delta = v3(*pix);
     const V3 surv = v3((int)p.depth >= p.lc[0] ? 1.0f : 0.0f, (int)p.depth >= p.lc[1] ? 1.0f : 0.0f,
                        (int)p.depth >= p.lc[2] ? 1.0f : 0.0f);
     const V3 wgt = delta * surv;
@@ -608,7 +583,66 @@ __device__ __forceinline__ bool adj_advance(TR& tr, const TraceArgs& a, const Ad
         }
     }
     p.depth++;
-    if (cont && p.depth < a.max_depth) return true;
+    return cont && p.depth < a.max_depth;
+}
+
+__device__ __forceinline__ uint4 hit_pack(const Hit& h)
+{
+    return make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+}
+__device__ __forceinline__ Hit hit_unpack(uint4 v)
+{
+    Hit h;
+    h.t = __uint_as_float(v.x);
+    h.prim = v.y;
+    h.slot = v.z;
+    h.kind = (int)v.w;
+    return h;
+}
+
+// One bounce of whichever pass the path is in, given the closest hit h of
+// its ray, then the bookkeeping: pass 1 ends -> pass 2 of the same sample
+// from the sample's first ray and RNG state; pass 2 ends -> the next sample
+// (the RNG continues where pass 1 left it).  pix: the pixel's delta and the
+// RNG salt at the sample's start; prim0: the salt at the end of pass 1.
+// With a hit log (w.log), pass 1 records its hits and pass 2 runs right
+// where pass 1 ends, from the log, without tracing: the same rays meet the
+// same hits, so the gradients are those of tracing them again.
+// Returns true while the pixel has a ray to trace.
+template <class TR>
+__device__ __forceinline__ bool adj_advance(TR& tr, const TraceArgs& a, const AdjWf& w, uint32_t pid, uint32_t x,
+                                            uint32_t y, const Hit& h, AdjPath& p, float4* pix, uint32_t* prim0)
+{
+    uint4* log = w.log ? w.log + (size_t)pid * a.max_depth : nullptr;
+    if (!p.replay) {
+        // pass 1: clamp bookkeeping, then the forward bounce
+        const bool found = h.kind != 0;
+        if (p.acc.x < 0.0f || p.acc.x > 1.0f) { p.lc[0] = (int)p.depth; p.T.x = 0.0f; }
+        if (p.acc.y < 0.0f || p.acc.y > 1.0f) { p.lc[1] = (int)p.depth; p.T.y = 0.0f; }
+        if (p.acc.z < 0.0f || p.acc.z > 1.0f) { p.lc[2] = (int)p.depth; p.T.z = 0.0f; }
+        p.acc = vclamp01(p.acc);
+        const V3 before = p.acc;
+        const bool cont = shade_bounce<false>(tr, a, p.depth, found, h, p.ray, p.acc, p.mask, p.g);  // no emitters
+        p.T = p.T + (p.acc - before);
+        if (log) log[p.depth] = hit_pack(h);
+        p.depth++;
+        if (cont && p.depth < a.max_depth) return true;
+        // pass 2 of the same sample: its first ray and RNG state again
+        const uint32_t bounces = p.depth;
+        *prim0 = __float_as_uint(p.g.salt);
+        p.g.salt = pix->w;
+        p.ray = primary_ray(a, x, y);
+        p.acc = splat(0.0f);
+        p.mask = splat(1.0f);
+        p.depth = 0;
+        p.replay = true;
+        if (!log) return true;
+        const V3 delta = v3(*pix);
+        while (adj_replay_bounce(tr, a, w, hit_unpack(log[p.depth]), delta, p) && p.depth < bounces) {
+        }
+    } else if (adj_replay_bounce(tr, a, w, h, v3(*pix), p)) {
+        return true;
+    }
     // sample finished: the RNG continues where pass 1 left it
     p.g.salt = __uint_as_float(*prim0);
     p.sample++;
@@ -652,7 +686,7 @@ __global__ void __launch_bounds__(256) wf_adj_shade(TraceArgs a, WfState s, AdjW
             h.prim = hr.y;
             h.slot = hr.z;
             h.kind = (int)hr.w;
-            again = adj_advance(tr, a, w, x, y, h, p, w.pix + pid, s.prim0 + pid);
+            again = adj_advance(tr, a, w, pid, x, y, h, p, w.pix + pid, s.prim0 + pid);
             if (again) adj_store(s, pid, p);
         }
         warp_append(again, pid, next, &s.count[qsel ^ 1]);
@@ -689,7 +723,7 @@ __global__ void __launch_bounds__(128) wf_adj_finish(TraceArgs a, WfState s, Adj
             Hit h;
             h.t = depth_tmax(p.depth);
             tr.trace(p.ray, h, false);
-            if (!adj_advance(tr, a, w, x, y, h, p, w.pix + pid, s.prim0 + pid)) break;
+            if (!adj_advance(tr, a, w, pid, x, y, h, p, w.pix + pid, s.prim0 + pid)) break;
         }
         qi = n > threads ? threads + atomicAdd(&s.count[2], 1u) : n;
     }

@@ -35,6 +35,8 @@ struct AdjWf {
     double* grad;          // [nm x 3 albedo][nm x 3 emission][3 camera position]
     uint32_t nm;
     float4* pix;           // per pixel: delta, RNG salt at the current sample's start
+    uint4* log;            // pass 1's closest hits of the current sample, max_depth per pixel
+                           // (pixel-major); nullptr = pass 2 traces its rays again
 };
 // Seeds every pixel with a finite delta and queues it in queue 0 (counts must be zero).
 cudaError_t wf_launch_adj_generate(const TraceArgs& a, const WfState& s, const AdjWf& w, cudaStream_t st);

@@ -43,6 +43,7 @@ EXPORTED_SYMBOLS = [
     "tracer_camera_init", "tracer_camera_init_startup", "tracer_camera_update", "tracer_camera_move",
     "tracer_camera_cursor", "tracer_camera_keys", "tracer_camera_script", "tracer_trace_whitted",
     "tracer_last_rounds", "tracer_measure_l2_read", "tracer_set_traversal_limit", "tracer_set_edge_sampling",
+    "tracer_set_adjoint_hit_log",
 ]
 PRESENT_PINGPONG, PRESENT_ACCUMULATE = 0, 1
 KEY_W, KEY_S, KEY_A, KEY_D, KEY_R, KEY_F = 1, 2, 4, 8, 16, 32
@@ -128,6 +129,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.tracer_set_timeout.argtypes = [vp, u32]
     lib.tracer_set_traversal_limit.argtypes = [vp, u32]
     lib.tracer_set_edge_sampling.argtypes = [vp, u32]
+    lib.tracer_set_adjoint_hit_log.argtypes = [vp, ctypes.c_uint64]
     lib.tracer_upload_scene.argtypes = [vp, ctypes.POINTER(SceneDesc)]
     lib.tracer_set_materials.argtypes = [vp, vp, u32]
     lib.tracer_trace.argtypes = [vp, vp, ctypes.POINTER(TraceParams), vp]
@@ -236,6 +238,10 @@ class Tracer:
     def set_edge_sampling(self, samples_per_edge: int):
         """Pieces per triangle edge of the camera gradient's boundary part (0 = off, the default)."""
         self._check(self.lib.tracer_set_edge_sampling(self.h, samples_per_edge))
+
+    def set_adjoint_hit_log(self, max_bytes: int):
+        """Device memory the wavefront adjoint may keep pass 1's hits in (0 = none: pass 2 traces again)."""
+        self._check(self.lib.tracer_set_adjoint_hit_log(self.h, max_bytes))
 
     @staticmethod
     def _fill_desc(d: SceneDesc, sc: S.Scene, tri_bvh=None, sphere_bvh=None) -> list:
