@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include "tracer_core.cuh"
+#include "tracer_cw8.cuh"
 #include "tracer_launch.h"
 #include "tracer_wavefront.h"
 
@@ -707,11 +708,16 @@ __global__ void __launch_bounds__(128) wf_adj_finish(TraceArgs a, WfState s, Adj
     for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
     const Stack stk{smem + threadIdx.x, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + threadIdx.x,
                     (int)blockDim.x, (int)a.stack_depth};
-    // closest hits with the plain traversal, which tests a hit leaf child as
-    // soon as its parent is visited: on short, latency-bound chains (c3's 256^2
-    // adjoint) 1.35 ms against 1.42 with the forward finishing kernel's
-    // pre-encoded traversal
+    // closest hits: the per-thread 8-wide traversal where the scene has one
+    // (c3's 256^2 adjoint: 0.47 ms against 0.74 with the plain binary
+    // traversal), else the plain traversal, which tests a hit leaf child as
+    // soon as its parent is visited (on c3's short, latency-bound chains it
+    // beat the pre-encoded binary traversal, 1.35 against 1.42 ms)
     Tracer<TIE, BVH, STATS> tr{a.sc, stk, cnt, a.status, a.trav_limit};
+    // triangle-only scenes with an 8-wide BVH: the forward finishing kernel's
+    // per-thread 8-wide traversal, its stack over the same shared memory
+    // (stack_depth 8-byte entries per thread; nothing here traces shadow rays)
+    const PairStack pstk{reinterpret_cast<int2*>(smem) + threadIdx.x, (int)blockDim.x, (int)a.stack_depth};
     const uint32_t threads = gridDim.x * blockDim.x;
     uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
     while (qi < n) {
@@ -722,7 +728,10 @@ __global__ void __launch_bounds__(128) wf_adj_finish(TraceArgs a, WfState s, Adj
         for (;;) {
             Hit h;
             h.t = depth_tmax(p.depth);
-            tr.trace(p.ray, h, false);
+            if (BVH && a.sc.tri_cw8 != nullptr)
+                closest_cw8<STATS>(a.sc, p.ray, h, pstk, a.status, a.trav_limit, cnt);
+            else
+                tr.trace(p.ray, h, false);
             if (!adj_advance(tr, a, w, pid, x, y, h, p, w.pix + pid, s.prim0 + pid)) break;
         }
         qi = n > threads ? threads + atomicAdd(&s.count[2], 1u) : n;
