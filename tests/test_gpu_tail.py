@@ -171,22 +171,35 @@ def test_graph_handover_replayed_for_other_frames(gpu_tracer):
 
 def test_auto_kernel_choice(gpu_tracer):
     """TRACER_KERNEL_AUTO: the wavefront (more than one launch) for BVH scenes
-    from 2^22 pixel x spp x depth, else the plain kernel (one launch);
-    linear-scan scenes plain."""
+    from 2^16 pixel x spp x depth when the scene has an 8-wide BVH (triangles
+    only; bvh_width 0 or 8), from 2^22 otherwise (bvh_width 2 asked for, or
+    spheres in the scene), else the plain kernel (one launch); linear-scan
+    scenes plain."""
     sc = soup_scene(5, 4000, extent=12.0, sigma=0.5)
+    sph = soup_scene(5, 4000, extent=12.0, sigma=0.5)
+    sph.spheres = S.random_spheres(9, 4)  # spheres: no 8-wide BVH
     fr = S.frame(S.look_at((0.0, 3.0, 30.0), (0.0, 0.0, 0.0), 40.0), 1.0, 0.7)
     gpu_tracer.set_profiling(True)
     try:
-        for bvh, (w, h, spp, depth), wavefront in ((True, (256, 256, 4, 4), False), (True, (512, 512, 4, 4), True),
-                                                   (False, (512, 512, 4, 4), False)):
-            if bvh:
+        for scene, width, (w, h, spp, depth), wavefront in (
+                ("tris", 0, (64, 64, 2, 4), False),        # 2^15
+                ("tris", 0, (128, 128, 1, 4), True),       # 2^16
+                ("tris", 0, (256, 256, 4, 4), True),
+                ("tris", 2, (256, 256, 4, 4), False),
+                ("tris", 2, (512, 512, 4, 4), True),
+                ("spheres", 0, (256, 256, 4, 4), False),
+                ("spheres", 0, (512, 512, 4, 4), True),
+                ("linear", 0, (512, 512, 4, 4), False)):
+            if scene == "tris":
                 gpu_tracer.upload_scene(sc)
+            elif scene == "spheres":
+                gpu_tracer.upload_scene(sph)
             else:
                 gpu_tracer.upload_scene(S.Scene(triangles=sc.triangles[:200], materials=sc.materials,
                                                 bvh=S.BVH_NONE))
             p = abi.Tracer.params(w, h, spp=spp, max_depth=depth, rr_start=2, sky=(1.0, 1.0, 1.0),
-                                  kernel=abi.KERNEL_AUTO)
+                                  kernel=abi.KERNEL_AUTO, bvh_width=width)
             gpu_tracer.trace(fr, p)
-            assert (gpu_tracer.timings()["launches"] > 1) == wavefront, (bvh, w, h, spp, depth)
+            assert (gpu_tracer.timings()["launches"] > 1) == wavefront, (scene, width, w, h, spp, depth)
     finally:
         gpu_tracer.set_profiling(False)

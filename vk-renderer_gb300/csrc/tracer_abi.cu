@@ -794,17 +794,23 @@ int tracer_trace(tracer_ctx* c, const tracer_frame* f, const tracer_trace_params
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown tie mode %d", p->tie_mode);
     if (p->tie_mode == TRACER_TIES_REFERENCE && c->scene.bvh)
         return fail(c, TRACER_ERR_INVALID_ARG, "reference ties depend on scan order and need a linear-scan scene");
-    // AUTO: the wavefront pays for itself on BVH scenes with enough path
-    // bounces in flight; the plain kernel wins on linear-scan scenes and small
-    // frames.  Measured (plain / wavefront ms): the reference's own 10-primitive
-    // frame 1.6 / 2.2; c1 scene 256^2 x 4 spp x depth 8 (2^21 bounces)
-    // 2.98 / 3.26, 512x288 x 4 x 8 (4.7M) 5.74 / 3.98, 1920x1080 x 16 x 8
-    // 225 / 91; c3 scene 256^2 x 4 x 4 (2^20) 0.59 / 0.90, 512^2 x 4 x 4
-    // (2^22) 1.44 / 1.20; c0 512^2 x 1 x 2 0.067 / 0.118.
+    // AUTO: the wavefront on BVH scenes with enough path bounces in flight --
+    // from 2^16 where the scene has an 8-wide BVH (its traversal, in the
+    // extend and finishing kernels, wins even on small frames), from 2^22
+    // otherwise; the plain kernel on linear-scan scenes and small frames.
+    // Measured (plain / wavefront ms), 8-wide: c3 scene 128^2 x 4 spp x
+    // depth 4 (2^18 bounces) 0.48 / 0.30, 256^2 x 4 x 4 0.59 / 0.38, 512^2
+    // 1.42 / 0.91; c1 scene 128^2 x 4 x 8 2.63 / 1.63, 256^2 x 4 x 8 2.95 /
+    // 1.83, 640x360 x 4 x 8 8.06 / 3.08, 1920x1080 x 16 x 8 222 / 58; c4
+    // scene 256^2 x 4 x 12 6.22 / 3.80.  Binary only: c0 (spheres) 512^2 x 1
+    // x 2 0.067 / 0.118; the reference's own 10-primitive frame (linear) 1.6
+    // / 2.2.
     const uint64_t bounces = (uint64_t)p->width * p->height * p->spp * p->max_depth;
+    const bool cw8_auto = c->scene.cw8 && (p->bvh_width == 0 || p->bvh_width == 8);
     const int kernel = p->kernel != TRACER_KERNEL_AUTO ? p->kernel
-                       : (c->scene.bvh && bounces >= (1ull << 22)) ? TRACER_KERNEL_WAVEFRONT
-                                                                   : TRACER_KERNEL_PLAIN;
+                       : (c->scene.bvh && bounces >= (cw8_auto ? (1ull << 16) : (1ull << 22)))
+                           ? TRACER_KERNEL_WAVEFRONT
+                           : TRACER_KERNEL_PLAIN;
     if (kernel != TRACER_KERNEL_PLAIN && kernel != TRACER_KERNEL_WAVEFRONT)
         return fail(c, TRACER_ERR_INVALID_ARG, "unknown kernel %d", p->kernel);
     uint32_t block = p->block ? p->block : 128;
