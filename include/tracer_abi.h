@@ -173,8 +173,9 @@ typedef struct tracer_scene_desc {
 #define TRACER_TIES_REFERENCE 0 /* Tracer.comp:382/:402/:418 scan-order rule; linear scan only */
 #define TRACER_TIES_STRICT 1    /* nearest (t, primitive id) below tmax; required with a BVH */
 
-#define TRACER_KERNEL_AUTO 0      /* WAVEFRONT for BVH scenes with >= 2^22 pixel x spp x depth, else PLAIN
-                                     (tracer_trace_adjoint: WAVEFRONT wherever it applies) */
+#define TRACER_KERNEL_AUTO 0      /* WAVEFRONT for BVH scenes with >= 2^16 pixel x spp x depth when the
+                                     scene has an 8-wide BVH (and bvh_width is 0 or 8), >= 2^22 otherwise;
+                                     else PLAIN (tracer_trace_adjoint: WAVEFRONT wherever it applies) */
 #define TRACER_KERNEL_PLAIN 1     /* one thread per pixel, nested sample/bounce loops */
 #define TRACER_KERNEL_WAVEFRONT 2 /* persistent extend kernel + shade kernel over path queues */
 
