@@ -367,6 +367,10 @@ constexpr int kCw8Postpone = 6;
 // (One primitive per sequential step and the owner found by shuffles
 // instead: 61.4 unshared, 60.1-60.4 at 8.)
 constexpr int kCw8SharedBelow = 12;
+// (Lanes whose ray is done and who hold no primitives taking their next ray
+// inside the node phase, rather than idling until the primitive phase ends:
+// 62.6 against 57.9 ms -- the fetch in every node step costs more than the
+// idle lanes.)
 
 // The extend kernel over the compressed 8-wide BVH (triangle scenes; strict
 // ties).  Same phases as wf_extend_bvh: idle lanes fetch rays; all lanes visit
@@ -411,49 +415,61 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     int sp = 0, nh = 0;
     const float4* nodes = nullptr;
     const float4* tris = nullptr;
+    // idle lanes take the next rays of the queue (warp-aggregated: one
+    // atomic per warp and call)
+    auto fetch = [&]() {
+        const unsigned need = __ballot_sync(full, !has && !exhausted);
+        if (!need) return;
+        const int leader = __ffs(need) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&s.count[2], (uint32_t)__popc(need));
+        base = __shfl_sync(full, base, leader);
+        if (has || exhausted) return;
+        const uint32_t qi = base + __popc(need & ((1u << lane) - 1u));
+        if (qi >= total) {
+            exhausted = true;
+            return;
+        }
+        pid = queue[qi];
+        scene = MULTI ? s.scene_of[pid] : 0;
+        const DevScene& sc = SCENE_ARGS(MULTI, a, slots, scene).sc;
+        const float4 ro = s.ray_o[pid];
+        const float4 rd = s.ray_d[pid];
+        ray = Ray{v3(ro), v3(rd)};
+        h.t = ro.w;
+        h.prim = 0;  // see accept_strict
+        h.kind = 0;
+        h.slot = 0;
+        steps = 0;
+        if (STATS) cnt.c[C_CLOSEST]++;
+        has = true;
+        if (isnan3(ray.d) || !(sc.n_tri_nodes > 0 && sc.nt > 0)) {
+            // no BVH work: NaN directions hit nothing; planes only
+            if (!isnan3(ray.d)) planes_pass<STATS>(sc, ray, h, cnt);
+            if (STATS && h.kind) cnt.c[C_HITS]++;
+            s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+            has = false;
+        } else {
+            cr = make_cw8ray(ray);
+            nodes = sc.tri_cw8;
+            tris = sc.tri_cw8_prims;
+            // the root: the one interior child (slot 0) of a group of its own
+            G = make_uint2(0u, (1u << (24 + (0u ^ cr.oct7))) | 1u);
+            sp = 0;
+        }
+    };
+    // a ray whose traversal is over and whose primitives are all tested:
+    // planes, then its result
+    auto finish_ray = [&]() {
+        const DevScene& sc = SCENE_ARGS(MULTI, a, slots, scene).sc;
+        planes_pass<STATS>(sc, ray, h, cnt);
+        if (STATS && h.kind) cnt.c[C_HITS]++;
+        s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
+        has = false;
+    };
     for (;;) {
         // 1) idle lanes take the next rays of the queue
-        const unsigned need = __ballot_sync(full, !has && !exhausted);
-        if (need) {
-            const int leader = __ffs(need) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&s.count[2], (uint32_t)__popc(need));
-            base = __shfl_sync(full, base, leader);
-            if (!has && !exhausted) {
-                const uint32_t qi = base + __popc(need & ((1u << lane) - 1u));
-                if (qi >= total) {
-                    exhausted = true;
-                } else {
-                    pid = queue[qi];
-                    scene = MULTI ? s.scene_of[pid] : 0;
-                    const DevScene& sc = SCENE_ARGS(MULTI, a, slots, scene).sc;
-                    const float4 ro = s.ray_o[pid];
-                    const float4 rd = s.ray_d[pid];
-                    ray = Ray{v3(ro), v3(rd)};
-                    h.t = ro.w;
-                    h.prim = 0;  // see accept_strict
-                    h.kind = 0;
-                    h.slot = 0;
-                    steps = 0;
-                    if (STATS) cnt.c[C_CLOSEST]++;
-                    has = true;
-                    if (isnan3(ray.d) || !(sc.n_tri_nodes > 0 && sc.nt > 0)) {
-                        // no BVH work: NaN directions hit nothing; planes only
-                        if (!isnan3(ray.d)) planes_pass<STATS>(sc, ray, h, cnt);
-                        if (STATS && h.kind) cnt.c[C_HITS]++;
-                        s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
-                        has = false;
-                    } else {
-                        cr = make_cw8ray(ray);
-                        nodes = sc.tri_cw8;
-                        tris = sc.tri_cw8_prims;
-                        // the root: the one interior child (slot 0) of a group of its own
-                        G = make_uint2(0u, (1u << (24 + (0u ^ cr.oct7))) | 1u);
-                        sp = 0;
-                    }
-                }
-            }
-        }
+        fetch();
         if (!__any_sync(full, has)) {
             if (__all_sync(full, exhausted)) break;
             continue;
@@ -522,13 +538,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
         }
         nh = 0;
         // 4) finished rays: planes and the result
-        if (has && (G.y & 0xFF000000u) == 0u && sp == 0) {
-            const DevScene& sc = SCENE_ARGS(MULTI, a, slots, scene).sc;
-            planes_pass<STATS>(sc, ray, h, cnt);
-            if (STATS && h.kind) cnt.c[C_HITS]++;
-            s.hit[pid] = make_uint4(__float_as_uint(h.t), h.prim, h.slot, (uint32_t)h.kind);
-            has = false;
-        }
+        if (has && (G.y & 0xFF000000u) == 0u && sp == 0) finish_ray();
     }
     if (STATS) flush_counters(a, cnt);
 }
