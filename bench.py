@@ -46,6 +46,15 @@ L2_FLUSH_BYTES = 256 << 20
 # rays.
 NCU_EXTEND_DRAM_BYTES_PER_RAY = 60.3
 
+# DRAM bytes of one replay of the c2 batch's graph (the bench's tuned shape:
+# 8-wide, 256 threads, hand-over at 1M paths), from one ncu capture of every
+# kernel of four replays (profiles/batch_c2_graph_launches.md): the extend
+# kernel's (21.4 GB read + 2.45 GB written) and all kernels' (42.0 + 14.5 GB;
+# wf_shade 20.4 + 9.8 GB).  The 2.1M triangles' 64-byte records and nodes
+# exceed L2, unlike c1's.
+NCU_BATCH_EXTEND_DRAM_BYTES = 23.85e9
+NCU_BATCH_ALL_DRAM_BYTES = 56.45e9
+
 
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -284,6 +293,8 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
     tr.close()
     decomp = batch_decomposition(local, wls, p_plain)
     pixels = sum(w.pixels for w in wls)
+    hbm, hbm_src = peaks()
+    k_bytes = algorithmic_bytes(st, pixels, 4)
     return {"metric": "batched Mrays/s (64 scenes, one CUDA-graph wavefront)", "value": rays / (ms_wf / 1e3) / 1e6,
             "unit": UNIT, "ms_per_step": ms_wf,
             "plain_per_scene": {"value": rays / (ms_plain / 1e3) / 1e6, "ms_per_step": ms_plain,
@@ -293,6 +304,14 @@ def batched_section(local: int, steps: int, warmup: int) -> dict:
             "triangles": int(sum(len(w.scene.triangles) for w in wls)),
             "autotuned": best, "autotune_candidates": len(table),
             "decomposition": decomp,
+            # canonical algorithmic bytes (the plain kernel's counts) over the
+            # whole replay, against measured HBM; DRAM traffic from ncu
+            "roofline": {"bound": "issue / L2 latency (extend kernel, 88.6 % of a replay); the scenes exceed L2",
+                         "achieved": k_bytes / (ms_wf / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": k_bytes / (ms_wf / 1e3) / 1e9 / hbm, "peak_source": hbm_src,
+                         "algorithmic_bytes_per_step": k_bytes, "traffic": NCU_BATCH_EXTEND_DRAM_BYTES,
+                         "kernel": "wf_extend_cw8 (MULTI)", "traffic_all_kernels": NCU_BATCH_ALL_DRAM_BYTES,
+                         "dram_gbs_all_kernels": NCU_BATCH_ALL_DRAM_BYTES / (ms_wf / 1e3) / 1e9},
             "config": {"workload": "c2-64scenes-tris-loguniform-1k-200k-res128-1024-4spp-d6-rr3-sah16",
                        "l2": "flushed before each timed step (256 MiB write)"}}
 
