@@ -1,6 +1,7 @@
 // Adjoint (reverse-mode) trace for sm_103a: gradients of an image loss with
 // respect to the material table's albedo and emission and to the camera
-// position, by path replay with O(1) state per path (no stored path vertices).
+// position, by path replay with O(1) state per path (the wavefront form
+// keeps the current sample's pass-1 hits so that pass 2 need not trace).
 //
 // The image is I = tonemap(accum / spp) + dither (Tracer.comp:585-590), accum
 // the sum of the samples' radiance (:578-581).  Given dL/dI per pixel:
@@ -424,9 +425,12 @@ __global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
 
 // ------------------------------------------------------ wavefront adjoint --
 // The same two passes per sample for scenes without emissive spheres, as
-// stages over the wavefront's path queue: the closest-hit rays of both passes
-// go through the forward renderer's extend kernel, and wf_adj_shade runs one
-// bounce of whichever pass a path is in.  A path's state between rounds:
+// stages over the wavefront's path queue: the closest-hit rays of pass 1 (and
+// of pass 2 when there is no hit log) go through the forward renderer's
+// extend kernel, and wf_adj_shade runs one bounce of whichever pass a path is
+// in; with the hit log, pass 2 runs whole where pass 1 ends (adj_advance).
+// The camera gradient's interior part is zero here (below); its boundary part
+// comes from the edge kernel.  A path's state between rounds:
 //   ray_o/ray_d  the ray to trace next (tmax in ray_o.w)
 //   acc          pass 1: acc; pass 2: the surviving prefix; .w the RNG salt
 //   mask         mask; .w the three last-clamp depths (10 bits each, +1)
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(128) k_adjoint(TraceArgs a, AdjArgs ga)
 //   pix          delta of the pixel; .w the RNG salt at the sample's start
 //   prim0        the RNG salt at the sample's end (pass 2 restores it)
 // Without emitters the camera position enters radiance only through which
-// primitives are hit, so its gradient is zero.
+// primitives are hit, so the interior part of its gradient is zero.
 
 __device__ __forceinline__ uint32_t lc_pack(const int lc[3])
 {
@@ -696,7 +700,8 @@ __global__ void __launch_bounds__(256) wf_adj_shade(TraceArgs a, WfState s, AdjW
 
 // The adjoint's finishing kernel (as wf_finish for the forward): each thread
 // runs queued paths to the end of their pixels -- both passes of every
-// remaining sample -- with the per-thread traversal for the closest hits.
+// remaining sample (pass 2 from the hit log when there is one) -- with the
+// per-thread traversal for the closest hits.
 template <int TIE, bool BVH, bool STATS>
 __global__ void __launch_bounds__(128) wf_adj_finish(TraceArgs a, WfState s, AdjWf w, int qsel)
 {
