@@ -470,6 +470,7 @@ def adjoint_section(local: int, steps: int) -> dict:
     tr.set_materials(base)
     fp64 = fp64_host_check(wl, target, g_alb, idx)
     campos = campos_check(tr, wl, p_run)
+    campos1 = campos_check(tr, wl, p_run, depth=1)
     tr.close()
     fwd = fwd_rays / (ms_fwd / 1e3) / 1e6
     # headline: the forward frame's rays per second of adjoint time, i.e.
@@ -489,29 +490,50 @@ def adjoint_section(local: int, steps: int) -> dict:
             "kernels": per_kernel,
             "grad_check": {"max_rel_err_vs_central_fd": max(rel), "step": 1e-3,
                            "max_rel_err_vs_richardson_fd": max(rel_r), "steps": [1e-3, 5e-4],
-                           "components": len(rel), "fp64_host": fp64, "camera_position": campos},
+                           "components": len(rel), "fp64_host": fp64, "camera_position": campos,
+                           "camera_position_depth1": campos1},
             "loss": L0,
             "config": {"workload": wl.name, "triangles": len(wl.scene.triangles), "materials": nm}}
 
 
-def campos_check(tr, wl, p) -> dict:
+def campos_check(tr, wl, p, depth=None) -> dict:
     """The camera-position gradient at c3 (its boundary part: triangle
     outlines moving across the point-sampled pixels) against central
-    differences of the GPU forward with common random numbers, for a linear
-    loss (fixed random weights per pixel, so dL/dI is exact at every camera
-    position), step h = 0.02, averaged over 16 x 16 sub-pixel offsets of every
-    sample point (the camera's dir moved along right and up by a fraction of
-    a pixel: the one-pixel box the boundary term differentiates).  The
-    differences count outline crossings of sample points; their standard
-    error comes from the spread of 16 interleaved subsets of the offsets,
-    and err_in_se is the gradient's distance from them in units of it.
-    Also the adjoint's time with the boundary part on."""
+    differences of the GPU forward with common random numbers, for two linear
+    losses (fixed weights per pixel and channel, so dL/dI is exact at every
+    camera position): N(0, 1) weights, and smooth positive ones (1 + sin +
+    cos over the image: outline motions add up instead of cancelling).  The
+    differences are averaged over 24 x 24 sub-pixel offsets of every sample
+    point (the camera's dir moved along right and up by a fraction of a
+    pixel: the one-pixel box the boundary term differentiates), at steps
+    h = 0.005 and 0.01 (on c3's ~2-pixel triangles a larger step lets a
+    sample point cross two outlines of one triangle and biases the quotient
+    towards zero); their standard error comes from 16 random groups of the
+    offsets, and err_in_se is the gradient's distance from them in units of
+    it.  Also the adjoint's time with the boundary part on.  depth: the path
+    depth to check at (None: the workload's); at depth 1 every outline that
+    moves the image is a primary one, the part the boundary term models."""
+    saved_depth = p.max_depth
+    if depth is not None:
+        p.max_depth = depth
+    try:
+        return _campos_check(tr, wl, p)
+    finally:
+        p.max_depth = saved_depth
+
+
+def _campos_check(tr, wl, p) -> dict:
     import numpy as np
     from vktrace import abi
     from vktrace import scene as S
+    W, H = wl.width, wl.height
     g = np.random.default_rng(5)
-    dl = np.zeros((wl.height, wl.width, 4), np.float32)
-    dl[:, 1:, :3] = g.normal(size=(wl.height, wl.width - 1, 3)).astype(np.float32)
+    weights = {"normal": np.zeros((H, W, 4), np.float32), "smooth": np.zeros((H, W, 4), np.float32)}
+    weights["normal"][:, 1:, :3] = g.normal(size=(H, W - 1, 3)).astype(np.float32)
+    yy, xx = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    for c in range(3):
+        weights["smooth"][:, :, c] = 1.0 + 0.5 * np.sin(2 * np.pi * (xx / W + c / 3.0)) + 0.5 * np.cos(2 * np.pi * yy / H)
+    weights["smooth"][:, 0] = 0.0  # column 0 is NaN by construction
     p.aov_mask = (1 << abi.AOV_RGBA32F) | (1 << abi.AOV_LINEAR)
     tr.trace(wl.frame, p)
     lin = tr.readback(abi.AOV_LINEAR)
@@ -519,9 +541,10 @@ def campos_check(tr, wl, p) -> dict:
     # with every input resident
     import torch
     nm = len(wl.scene.materials)
-    dl_d, lin_d = torch.from_numpy(dl).cuda(), torch.from_numpy(lin).cuda()
+    dl_d, lin_d = torch.from_numpy(weights["normal"]).cuda(), torch.from_numpy(lin).cuda()
     outs = [torch.zeros((nm, 3), device="cuda"), torch.zeros((nm, 3), device="cuda"), torch.zeros(3, device="cuda")]
     stream = torch.cuda.current_stream()
+    grads = {}
     tr.set_edge_sampling(4)
     try:
         call = lambda: tr.trace_adjoint(wl.frame, p, dl_d.data_ptr(), lin_d.data_ptr(),
@@ -538,44 +561,50 @@ def campos_check(tr, wl, p) -> dict:
         torch.cuda.synchronize()
         tr.synchronize()
         ms_edges = a.elapsed_time(b) / 5
-        _, _, gc = tr.trace_adjoint(wl.frame, p, dl, lin, num_materials=nm)
+        for name, dl in weights.items():
+            _, _, gc = tr.trace_adjoint(wl.frame, p, dl, lin, num_materials=nm)
+            grads[name] = [float(v) for v in gc]
     finally:
         tr.set_edge_sampling(0)
-    h, ks = 0.02, 16
-    out = {"loss": "linear, N(0,1) weights per pixel and channel", "step": h, "subpixel_offsets": ks * ks,
-           "gradient": [float(v) for v in gc], "fd": [], "standard_error": [], "events": [], "err_in_se": [],
-           "adjoint_ms_with_boundary_part": ms_edges,
+    steps, ks = (0.005, 0.01), 24
+    out = {"losses": {"normal": "N(0,1) weights per pixel and channel",
+                      "smooth": "1 + 0.5 sin(2 pi (x/W + c/3)) + 0.5 cos(2 pi y/H) per pixel and channel"},
+           "max_depth": int(p.max_depth), "steps": list(steps), "subpixel_offsets": ks * ks,
+           "gradient": grads, "fd": {}, "adjoint_ms_with_boundary_part": ms_edges,
            "note": "boundary part on (tracer_set_edge_sampling 4; off by default): primary-visibility edge "
                    "sampling; outlines seen only by bounce rays are not modelled"}
     base = np.array(wl.frame, S.FRAME).reshape(())
     pos0 = np.array(base["camera"]["pos"], np.float64)
-    for axis in range(3):
-        step = float(np.float32(pos0[axis] + h) - np.float32(pos0[axis] - h))
-        per = np.zeros((ks, ks))
-        ev = 0
-        for i in range(ks):
-            for j in range(ks):
-                ox, oy = (i + 0.5) / ks - 0.5, (j + 0.5) / ks - 0.5
-                imgs = []
-                for sgn in (1.0, -1.0):
-                    f = base.copy()
-                    pos = pos0.copy()
-                    pos[axis] += sgn * h
-                    f["camera"]["pos"] = pos.astype(np.float32)
-                    cam = f["camera"]
-                    cam["dir"] = (cam["dir"].astype(np.float64) + cam["right"] * (2.0 * ox / wl.width)
-                                  + cam["up"] * (2.0 * oy / wl.height)).astype(np.float32)
-                    tr.trace(f, p)
-                    imgs.append(tr.readback(abi.AOV_RGBA32F))
-                d = ((imgs[0][:, 1:, :3].astype(np.float64) - imgs[1][:, 1:, :3]) * dl[:, 1:, :3]).sum(-1) / step
-                per[i, j] = d.sum()
-                ev += int((d != 0).sum())
-        subs = [per[a::4, b::4].mean() for a in range(4) for b in range(4)]
-        fd, se = float(per.mean()), float(np.std(subs, ddof=1) / 4.0)
-        out["fd"].append(fd)
-        out["standard_error"].append(se)
-        out["events"].append(ev)
-        out["err_in_se"].append(abs(float(gc[axis]) - fd) / se if se > 0 else None)
+    groups = np.random.default_rng(1).permutation(ks * ks).reshape(16, -1)
+    for h in steps:
+        rows = {name: {"fd": [], "standard_error": [], "err_in_se": []} for name in weights}
+        for axis in range(3):
+            step = float(np.float32(pos0[axis] + h) - np.float32(pos0[axis] - h))
+            per = {name: np.zeros(ks * ks) for name in weights}
+            for i in range(ks):
+                for j in range(ks):
+                    ox, oy = (i + 0.5) / ks - 0.5, (j + 0.5) / ks - 0.5
+                    imgs = []
+                    for sgn in (1.0, -1.0):
+                        f = base.copy()
+                        pos = pos0.copy()
+                        pos[axis] += sgn * h
+                        f["camera"]["pos"] = pos.astype(np.float32)
+                        cam = f["camera"]
+                        cam["dir"] = (cam["dir"].astype(np.float64) + cam["right"] * (2.0 * ox / W)
+                                      + cam["up"] * (2.0 * oy / H)).astype(np.float32)
+                        tr.trace(f, p)
+                        imgs.append(tr.readback(abi.AOV_RGBA32F)[:, 1:, :3].astype(np.float64))
+                    d = (imgs[0] - imgs[1]) / step
+                    for name, dl in weights.items():
+                        per[name][i * ks + j] = (d * dl[:, 1:, :3]).sum()
+            for name in weights:
+                fd = float(per[name].mean())
+                se = float(np.std([per[name][q].mean() for q in groups], ddof=1) / 4.0)
+                rows[name]["fd"].append(fd)
+                rows[name]["standard_error"].append(se)
+                rows[name]["err_in_se"].append(abs(grads[name][axis] - fd) / se if se > 0 else None)
+        out["fd"][str(h)] = rows
     return out
 
 
