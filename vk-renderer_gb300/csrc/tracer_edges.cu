@@ -57,26 +57,30 @@ __device__ __forceinline__ bool closest(TR& tr, const TraceArgs& a, const PairSt
     return tr.trace(ray, h, false);
 }
 
-// The forward value of pixel (x, y) for a primary ray through image point
-// (ux, uy) instead of the pixel's own sample point: every sample (the
-// pixel's random numbers) through the radiance loop (Tracer.comp:433-553),
-// Reinhard, gamma 1/2.2 and the dither, as resolve_pixel (:578-590).
+// The forward value of pixel (x, y) for the primary ray r (through another
+// image point than the pixel's own sample point) whose closest hit h0 is
+// given (found0: it hit): every sample (the pixel's random numbers) through
+// the radiance loop (Tracer.comp:433-553), Reinhard, gamma 1/2.2 and the
+// dither, as resolve_pixel (:578-590).  Every sample starts with the same
+// primary ray, so its hit is traced once, by the caller.
 template <class TR>
-__device__ __forceinline__ V3 pixel_value_at(TR& tr, const TraceArgs& a, const PairStack& pstk, uint32_t x,
-                                             uint32_t y, float ux, float uy, Counters& cnt)
+__device__ __forceinline__ V3 pixel_value_from(TR& tr, const TraceArgs& a, const PairStack& pstk, uint32_t x,
+                                               uint32_t y, const Ray& r, bool found0, const Hit& h0, Counters& cnt)
 {
     Rng g;
     seed_rng(a, x, y, g);
-    const Ray r = primary_ray_at(a, ux, uy);
     V3 accum = splat(0.0f);
     for (uint32_t s = 0; s < a.spp; ++s) {
         V3 acc = splat(0.0f), mask = splat(1.0f);
         Ray ray = r;
         for (uint32_t depth = 0; depth < a.max_depth; ++depth) {
             acc = vclamp01(acc);
-            Hit h;
-            h.t = depth_tmax(depth);
-            const bool found = closest(tr, a, pstk, ray, h, cnt);
+            Hit h = h0;
+            bool found = found0;
+            if (depth > 0) {
+                h.t = depth_tmax(depth);
+                found = closest(tr, a, pstk, ray, h, cnt);
+            }
             if (!shade_bounce(tr, a, depth, found, h, ray, acc, mask, g)) break;
         }
         accum = accum + acc;
@@ -201,8 +205,12 @@ __global__ void __launch_bounds__(128) k_edge_campos(TraceArgs a, EdgeArgs e)
                                 Hit hin;
                                 hin.t = depth_tmax(0);
                                 if (closest(tr, a, pstk, rin, hin, cnt) && hin.prim == tri_id) {
-                                    const V3 vin = pixel_value_at(tr, a, pstk, px, py, ix, iy, cnt);
-                                    const V3 vout = pixel_value_at(tr, a, pstk, px, py, ox, oy, cnt);
+                                    const Ray rout = primary_ray_at(a, ox, oy);
+                                    Hit hout;
+                                    hout.t = depth_tmax(0);
+                                    const bool fout = closest(tr, a, pstk, rout, hout, cnt);
+                                    const V3 vin = pixel_value_from(tr, a, pstk, px, py, rin, true, hin, cnt);
+                                    const V3 vout = pixel_value_from(tr, a, pstk, px, py, rout, fout, hout, cnt);
                                     w = dl.x * (vin.x - vout.x) + dl.y * (vin.y - vout.y) + dl.z * (vin.z - vout.z);
                                 }
                             }
