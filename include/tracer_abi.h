@@ -289,8 +289,8 @@ int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* byt
  * sample point (edge sampling of primary visibility; outlines seen only by
  * bounce rays, and sphere outlines, are not included).  The boundary part
  * re-evaluates every pixel an outline crosses on both sides of it, which on
- * the 10k-triangle soup at 256^2 x 4 spp costs about seven times the rest of
- * the adjoint (3.5 against 0.5 ms). */
+ * the 10k-triangle soup at 256^2 x 4 spp costs about 1.5 times the rest of
+ * the adjoint (0.8 against 0.5 ms). */
 int tracer_trace_adjoint(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
                          const float* dL_dimage, const float* linear_image, float* d_albedo, float* d_emission,
                          float* d_campos, void* cuda_stream);

@@ -87,8 +87,12 @@ struct AdjBuffers {
     DevBuf<float> gradf;  // the same, rounded to float for the outputs
     DevBuf<float4> pix;   // wavefront form: per-pixel delta and sample-start RNG state
     DevBuf<uint4> log;    // wavefront form: pass 1's closest hits of the current sample, per pixel
+    DevBuf<float4> segs;  // boundary term: the visible outline parts the edge walk hands over
+    DevBuf<uint32_t> nsegs;
     void release()
     {
+        segs.release();
+        nsegs.release();
         log.release();
         pix.release();
         dldi.release();
@@ -1863,12 +1867,20 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
     }
     // the camera's boundary term: triangle outlines moving across pixels
     if (e == cudaSuccess && d_campos && s.nt > 0 && c->edge_samples > 0) {
-        EdgeArgs ea{dldi, ab.grad.p + 6 * (size_t)s.nm, {}, c->edge_samples, 0.01f};
+        // room for 16 visible parts per edge piece on average (c3: 640k parts,
+        // 31 MB); parts beyond it are evaluated by the walk itself
+        const uint64_t cap64 = std::min<uint64_t>(16ull * s.nt * 3u * c->edge_samples, 1ull << 25);
+        const uint32_t cap = (uint32_t)std::max<uint64_t>(cap64, 1u << 16);
+        e = dalloc(ab.segs, 3 * (size_t)cap);
+        if (e == cudaSuccess) e = dalloc(ab.nsegs, 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ab.nsegs.p, 0, sizeof(uint32_t), st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "boundary-term buffers");
+        EdgeArgs ea{dldi, ab.grad.p + 6 * (size_t)s.nm, {}, c->edge_samples, 0.01f, ab.segs.p, ab.nsegs.p, cap};
         if (!camera_inverse(f->camera, ea.binv)) return fail(c, TRACER_ERR_INVALID_ARG, "degenerate camera basis");
         TraceArgs ae = a;
         ae.stack_depth = stack;  // the binary traversal's
         e = launch_edge_campos(ae, ea, p->tie_mode, s.bvh ? 1 : 0, st);
-        c->last_launches += 1;
+        c->last_launches += 2;
     }
     if (c->profiling) cudaEventRecord(c->prof_end, st);
     if (e == cudaSuccess) e = launch_grad_to_float(ab.grad.p, ab.gradf.p, (uint32_t)ng, st);

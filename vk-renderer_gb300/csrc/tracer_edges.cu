@@ -105,7 +105,52 @@ __device__ __forceinline__ V3 cam_coeffs(const EdgeArgs& e, const TraceArgs& a, 
               e.binv[6] * Y.x + e.binv[7] * Y.y + e.binv[8] * Y.z);
 }
 
-// One thread per (triangle edge, piece of it); block sums in FP64.
+// The loss weight of one visible outline part of pixel (px, py): dL/dI .
+// (I_inside - I_outside), the pixel evaluated for primary rays through the
+// inside point (ix, iy), whose closest hit hin is known, and the outside
+// point (ox, oy).
+template <class TR>
+__device__ __forceinline__ float part_weight(TR& tr, const TraceArgs& a, const PairStack& pstk, const EdgeArgs& e,
+                                             uint32_t px, uint32_t py, float ix, float iy, float ox, float oy,
+                                             const Hit& hin, Counters& cnt)
+{
+    const float4 dl = __ldg(e.dldi + (size_t)py * a.width + px);
+    const Ray rin = primary_ray_at(a, ix, iy);
+    const Ray rout = primary_ray_at(a, ox, oy);
+    Hit hout;
+    hout.t = depth_tmax(0);
+    const bool fout = closest(tr, a, pstk, rout, hout, cnt);
+    const V3 vin = pixel_value_from(tr, a, pstk, px, py, rin, true, hin, cnt);
+    const V3 vout = pixel_value_from(tr, a, pstk, px, py, rout, fout, hout, cnt);
+    return dl.x * (vin.x - vout.x) + dl.y * (vin.y - vout.y) + dl.z * (vin.z - vout.z);
+}
+
+// Block sum of the three camera-axis contributions in FP64, added to e.gcam.
+__device__ __forceinline__ void add_contrib(const EdgeArgs& e, const float (&contrib)[3], double (&red)[3][4])
+{
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        double v = (double)(isfinite(contrib[j]) ? contrib[j] : 0.0f);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+        if ((tid & 31) == 0) red[j][tid >> 5] = v;
+    }
+    __syncthreads();
+    if (tid < 3) {
+        const double v = red[tid][0] + red[tid][1] + red[tid][2] + red[tid][3];
+        if (v != 0.0) atomicAdd(e.gcam + tid, v);
+    }
+}
+
+// A visible outline part handed from the walk to k_edge_values: 3 float4 =
+// (inside point, outside point) (inside hit t, prim, slot, px | py << 16)
+// (the part's velocity factors n . du/dc_j times its length, j = x, y, z).
+constexpr uint32_t kEdgeSegFloat4 = 3;
+
+// The walk: one thread per (triangle edge, piece of it); the visible parts
+// it finds go to e.segs (or, without room there, are evaluated here);
+// block sums in FP64.
 template <int TIE, bool BVH>
 __global__ void __launch_bounds__(128) k_edge_campos(TraceArgs a, EdgeArgs e)
 {
@@ -192,45 +237,50 @@ __global__ void __launch_bounds__(128) k_edge_campos(TraceArgs a, EdgeArgs e)
                         const float ux = vx - 0.5f + tm * dx, uy = vy - 0.5f + tm * dy;
                         if (ux >= -0.5f && ux < (float)a.width - 0.5f && uy >= -0.5f && uy < (float)a.height - 0.5f) {
                             const uint32_t px = (uint32_t)floorf(ux + 0.5f), py = (uint32_t)floorf(uy + 0.5f);
-                            const float4 dl = __ldg(e.dldi + (size_t)py * a.width + px);
                             const float eps = e.offset_px;
                             const float ix = ux - eps * nx, iy = uy - eps * ny, ox = ux + eps * nx, oy = uy + eps * ny;
                             // the outline is visible here only if the inside ray sees this
                             // triangle: it faces the ray (the one-sided test's det, no
                             // trace needed) and nothing is in front of it; otherwise
                             // both sides see the same and there is nothing to trace
-                            float w = 0.0f;
                             const Ray rin = primary_ray_at(a, ix, iy);
                             if (dot(e1, cross(rin.d, e2)) >= EPSILON) {
                                 Hit hin;
                                 hin.t = depth_tmax(0);
                                 if (closest(tr, a, pstk, rin, hin, cnt) && hin.prim == tri_id) {
-                                    const Ray rout = primary_ray_at(a, ox, oy);
-                                    Hit hout;
-                                    hout.t = depth_tmax(0);
-                                    const bool fout = closest(tr, a, pstk, rout, hout, cnt);
-                                    const V3 vin = pixel_value_from(tr, a, pstk, px, py, rin, true, hin, cnt);
-                                    const V3 vout = pixel_value_from(tr, a, pstk, px, py, rout, fout, hout, cnt);
-                                    w = dl.x * (vin.x - vout.x) + dl.y * (vin.y - vout.y) + dl.z * (vin.z - vout.z);
-                                }
-                            }
-                            if (w != 0.0f && isfinite(w)) {
-                                // the 3D point (1 / lambda is linear along the image)
-                                const float sm = s0 + tm * (s1 - s0);
-                                const float tt = sm * qa.x / ((1.0f - sm) * qb.x + sm * qa.x);
-                                const V3 X = A + tt * (B - A);
-                                const V3 q = cam_coeffs(e, a, X);
-                                const float il = 1.0f / q.x;
-                                const float seg = (t1 - t0) * (s1 - s0) * len;
+                                    // velocity factors of the part: (n . du/dc_j) * its length,
+                                    // at the 3D point (1 / lambda is linear along the image)
+                                    float vel[3];
+                                    const float sm = s0 + tm * (s1 - s0);
+                                    const float tt = sm * qa.x / ((1.0f - sm) * qb.x + sm * qa.x);
+                                    const V3 X = A + tt * (B - A);
+                                    const V3 q = cam_coeffs(e, a, X);
+                                    const float il = 1.0f / q.x;
+                                    const float seg = (t1 - t0) * (s1 - s0) * len;
 #pragma unroll
-                                for (int j = 0; j < 3; ++j) {
-                                    // dY/dc_j = -e_j / (aspect, 1, aspect)_j; dq = binv dY
-                                    const float m = (j == 1) ? 1.0f : a.fr.aspect;
-                                    const float dlam = -e.binv[0 + j] / m, dmu = -e.binv[3 + j] / m,
-                                                dnu = -e.binv[6 + j] / m;
-                                    const float dux = (dmu * q.x - q.y * dlam) * il * il * hw;
-                                    const float duy = (dnu * q.x - q.z * dlam) * il * il * hh;
-                                    contrib[j] += w * (nx * dux + ny * duy) * seg;
+                                    for (int j = 0; j < 3; ++j) {
+                                        // dY/dc_j = -e_j / (aspect, 1, aspect)_j; dq = binv dY
+                                        const float m = (j == 1) ? 1.0f : a.fr.aspect;
+                                        const float dlam = -e.binv[0 + j] / m, dmu = -e.binv[3 + j] / m,
+                                                    dnu = -e.binv[6 + j] / m;
+                                        const float dux = (dmu * q.x - q.y * dlam) * il * il * hw;
+                                        const float duy = (dnu * q.x - q.z * dlam) * il * il * hh;
+                                        vel[j] = (nx * dux + ny * duy) * seg;
+                                    }
+                                    const uint32_t at = e.segs ? atomicAdd(e.nsegs, 1u) : 0xFFFFFFFFu;
+                                    if (at < e.seg_cap) {
+                                        float4* r = e.segs + (size_t)kEdgeSegFloat4 * at;
+                                        r[0] = make_float4(ix, iy, ox, oy);
+                                        r[1] = make_float4(hin.t, __uint_as_float(hin.prim), __uint_as_float(hin.slot),
+                                                           __uint_as_float(px | py << 16));
+                                        r[2] = make_float4(vel[0], vel[1], vel[2], 0.0f);
+                                    } else {
+                                        const float w = part_weight(tr, a, pstk, e, px, py, ix, iy, ox, oy, hin, cnt);
+                                        if (w != 0.0f && isfinite(w)) {
+#pragma unroll
+                                            for (int j = 0; j < 3; ++j) contrib[j] += w * vel[j];
+                                        }
+                                    }
                                 }
                             }
                         }
@@ -247,18 +297,46 @@ __global__ void __launch_bounds__(128) k_edge_campos(TraceArgs a, EdgeArgs e)
             }
         }
     }
+    add_contrib(e, contrib, red);
+}
+
+// The visible parts the walk handed over: one per thread (grid-stride), the
+// pixel on both sides of each; block sums in FP64.
+template <int TIE, bool BVH>
+__global__ void __launch_bounds__(128) k_edge_values(TraceArgs a, EdgeArgs e)
+{
+    extern __shared__ int smem[];
+    __shared__ double red[3][4];
+    const int tid = threadIdx.x;
+    Counters cnt;
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        double v = (double)(isfinite(contrib[j]) ? contrib[j] : 0.0f);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
-        if ((tid & 31) == 0) red[j][tid >> 5] = v;
+    for (int k = 0; k < C_COUNT; ++k) cnt.c[k] = 0;
+    Tracer<TIE, BVH, false> tr{a.sc,
+                               Stack{smem + tid, reinterpret_cast<float*>(smem + (size_t)a.stack_depth * blockDim.x) + tid,
+                                     (int)blockDim.x, (int)a.stack_depth},
+                               cnt, a.status, a.trav_limit};
+    const PairStack pstk{reinterpret_cast<int2*>(smem + 2 * (size_t)a.stack_depth * blockDim.x) + tid,
+                         (int)blockDim.x, (int)a.stack_depth};
+    float contrib[3] = {0.0f, 0.0f, 0.0f};
+    const uint32_t found = *e.nsegs;
+    const uint32_t n = found < e.seg_cap ? found : e.seg_cap;
+    for (uint32_t r = blockIdx.x * blockDim.x + tid; r < n; r += gridDim.x * blockDim.x) {
+        const float4* rec = e.segs + (size_t)kEdgeSegFloat4 * r;
+        const float4 pts = rec[0], hr = rec[1], vel = rec[2];
+        Hit hin;
+        hin.t = hr.x;
+        hin.prim = __float_as_uint(hr.y);
+        hin.slot = __float_as_uint(hr.z);
+        hin.kind = 1;
+        const uint32_t pp = __float_as_uint(hr.w);
+        const float w = part_weight(tr, a, pstk, e, pp & 0xFFFFu, pp >> 16, pts.x, pts.y, pts.z, pts.w, hin, cnt);
+        if (w != 0.0f && isfinite(w)) {
+            contrib[0] += w * vel.x;
+            contrib[1] += w * vel.y;
+            contrib[2] += w * vel.z;
+        }
     }
-    __syncthreads();
-    if (tid < 3) {
-        const double v = red[tid][0] + red[tid][1] + red[tid][2] + red[tid][3];
-        if (v != 0.0) atomicAdd(e.gcam + tid, v);
-    }
+    add_contrib(e, contrib, red);
 }
 
 template <int TIE, bool BVH>
@@ -273,6 +351,12 @@ static cudaError_t edge_t(const TraceArgs& a, const EdgeArgs& e, cudaStream_t st
     if (blocks == 0) return cudaSuccess;
     if (blocks > 0x7FFFFFFFull) return cudaErrorInvalidValue;
     k<<<(uint32_t)blocks, block, smem, st>>>(a, e);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess || !e.segs) return err;
+    auto kv = k_edge_values<TIE, BVH>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint64_t vb = ((uint64_t)e.seg_cap + block - 1) / block;
+    kv<<<(uint32_t)(vb < 65535 ? vb : 65535), block, smem, st>>>(a, e);
     return cudaGetLastError();
 }
 
