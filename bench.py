@@ -428,8 +428,14 @@ def adjoint_section(local: int, steps: int) -> dict:
     ms_fwd = timed(lambda: tr.trace(wl.frame, p_run, sptr))
     adj = lambda: tr.trace_adjoint(wl.frame, p_run, dl_d.data_ptr(), lin_d.data_ptr(),
                                    outputs=(ga.data_ptr(), ge.data_ptr(), gc.data_ptr()), stream=sptr)
-    ms_adj = timed(adj)  # AUTO: the wavefront (c3 has no emissive spheres)
+    ms_adj = timed(adj)  # AUTO: the wavefront (c3 has no emissive spheres); pure path replay
     adj_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+    # the opt-in hit log: pass 1's hits of the current sample kept (16 B x
+    # depth per pixel) so that pass 2 traces nothing; the same gradients
+    tr.set_adjoint_hit_log(4 << 30)
+    ms_log = timed(adj)
+    log_rays = sum(tr.stats()[k] for k in ("closest_rays", "shadow_rays"))
+    tr.set_adjoint_hit_log(0)
     # both adjoint forms on the same inputs, for comparison: forward rays per
     # second of each, and the rays each traced
     per_kernel = {}
@@ -474,9 +480,9 @@ def adjoint_section(local: int, steps: int) -> dict:
     tr.close()
     fwd = fwd_rays / (ms_fwd / 1e3) / 1e6
     # headline: the forward frame's rays per second of adjoint time, i.e.
-    # adjoint speed against forward speed on the same frame; beside it the
-    # rays the adjoint traced (pass 1 once more, and pass 2 too unless it
-    # replays pass 1's logged hits)
+    # adjoint speed against forward speed on the same frame, by pure path
+    # replay (the default); beside it the rays the adjoint traced (both
+    # passes) and the opt-in hit log's figures
     adjv = fwd_rays / (ms_adj / 1e3) / 1e6
     replay = adj_rays / (ms_adj / 1e3) / 1e6
     return {"metric": "adjoint Mrays/s (c3, path replay; forward rays per adjoint second)", "value": adjv,
@@ -484,8 +490,12 @@ def adjoint_section(local: int, steps: int) -> dict:
             "forward": {"value": fwd, "ms_per_step": ms_fwd, "rays_per_step": fwd_rays},
             "ratio_adjoint_to_forward": ms_fwd / ms_adj,
             "traced_rays": {"rays_per_step": adj_rays, "mrays_per_s": replay,
-                            "ratio_to_forward_mrays_per_s": replay / fwd,
-                            "pass2_from_hit_log": bool(adj_rays < 2 * fwd_rays)},
+                            "ratio_to_forward_mrays_per_s": replay / fwd},
+            "with_hit_log": {"value": fwd_rays / (ms_log / 1e3) / 1e6, "ms_per_step": ms_log,
+                             "ratio_adjoint_to_forward": ms_fwd / ms_log, "traced_rays": log_rays,
+                             "note": "opt-in (tracer_set_adjoint_hit_log): pass 1's hits of the current sample "
+                                     "kept, 16 B x max_depth per pixel, so pass 2 traces nothing; off by default "
+                                     "(pure path replay, no stored path vertices)"},
             "kernel": "auto (wavefront: no emissive spheres)",
             "kernels": per_kernel,
             "grad_check": {"max_rel_err_vs_central_fd": max(rel), "step": 1e-3,

@@ -274,12 +274,11 @@ int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* byt
  * waits (bounded) for the result, with device outputs it is asynchronous on
  * cuda_stream.  Path replay: every sample is traced again (pass 1, giving
  * its radiance) and then replayed with the gradient terms (pass 2, the same
- * rays): the per-pixel form traces pass 2's rays too; the wavefront form
- * (scenes without emissive spheres) keeps pass 1's closest hits of each
- * pixel's current sample (16 bytes x max_depth per pixel, within the limit
- * tracer_set_adjoint_hit_log sets; beyond it pass 2 traces) and pass 2 reads
- * them instead of tracing.  The Russian-roulette normalisation is treated as
- * a constant.  Materials of spheres and planes (stored inline) get no gradient.
+ * rays, traced again: no path vertices are stored).  As an option
+ * (tracer_set_adjoint_hit_log), the wavefront form (scenes without emissive
+ * spheres) keeps pass 1's closest hits of each pixel's current sample (16
+ * bytes x max_depth per pixel) and pass 2 reads them instead of tracing.
+ * The Russian-roulette normalisation is treated as a constant.  Materials of spheres and planes (stored inline) get no gradient.
  * d_campos is the interior part (the camera position enters next-event
  * shading through the view vector and the hit points: the derivative of the
  * point-sampled image away from outlines, zero for scenes without emissive
@@ -289,8 +288,8 @@ int tracer_device_image(tracer_ctx* ctx, int aov, void** device_ptr, size_t* byt
  * sample point (edge sampling of primary visibility; outlines seen only by
  * bounce rays, and sphere outlines, are not included).  The boundary part
  * re-evaluates every pixel an outline crosses on both sides of it, which on
- * the 10k-triangle soup at 256^2 x 4 spp costs about 1.5 times the rest of
- * the adjoint (0.8 against 0.5 ms). */
+ * the 10k-triangle soup at 256^2 x 4 spp costs about as much as the rest of
+ * the adjoint (1.0 against 0.86 ms). */
 int tracer_trace_adjoint(tracer_ctx* ctx, const tracer_frame* frame, const tracer_trace_params* params,
                          const float* dL_dimage, const float* linear_image, float* d_albedo, float* d_emission,
                          float* d_campos, void* cuda_stream);
@@ -306,9 +305,10 @@ int tracer_set_edge_sampling(tracer_ctx* ctx, uint32_t samples_per_edge);
 /* Device memory the wavefront adjoint may keep pass 1's closest hits in
  * (width x height x max_depth x 16 bytes; allocated on first use and kept
  * for later adjoints of the context): pass 2 then replays them without
- * tracing, which halves the adjoint's traced rays with the same gradients.
- * A trace whose hits would exceed the limit traces pass 2 instead.  0 = never
- * keep them (frees the buffer); default 4 GiB.  No counterpart in the
+ * tracing, which halves the adjoint's traced rays with the same gradients
+ * (c3: 0.48 against 0.79 ms).  A trace whose hits would exceed the limit
+ * traces pass 2 instead.  0 = never keep them, the default: pure path replay,
+ * no stored path vertices (frees the buffer).  No counterpart in the
  * reference. */
 int tracer_set_adjoint_hit_log(tracer_ctx* ctx, uint64_t max_bytes);
 

@@ -148,11 +148,11 @@ def test_adjoint_vs_fp64_host(gpu_tracer):
 def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case, hit_log):
     """Scenes without emitters take the wavefront adjoint (closest hits
     through the forward extend kernel); the per-pixel adjoint kernel traces
-    both passes of every sample.  With the hit log (the default) the
-    wavefront traces pass 1 only and replays pass 2 from the logged hits:
-    exactly half the per-pixel kernel's rays and hits; without it (limit 0)
-    it traces both passes: the same counts.  Gradients are equal up to the
-    order of the FP64 sums either way."""
+    both passes of every sample.  With the hit log (opt-in) the wavefront
+    traces pass 1 only and replays pass 2 from the logged hits: exactly half
+    the per-pixel kernel's rays and hits; without it (limit 0, the default:
+    pure path replay) it traces both passes: the same counts.  Gradients are
+    equal up to the order of the FP64 sums either way."""
     tr = gpu_tracer
     tr.set_adjoint_hit_log((4 << 30) if hit_log else 0)
     sc = _scene(seed=21, n=2000, nm=16)
@@ -195,7 +195,7 @@ def test_wavefront_adjoint_equals_per_pixel(gpu_tracer, case, hit_log):
             scale = float(np.max(np.abs(a))) if np.any(a) else 1.0
             np.testing.assert_allclose(b, a, rtol=1e-5, atol=1e-7 * scale, err_msg=str(key))
         assert np.any(wa != 0)
-    tr.set_adjoint_hit_log(4 << 30)
+    tr.set_adjoint_hit_log(0)  # the default: pure replay
 
 
 def _nee_scene(kind):

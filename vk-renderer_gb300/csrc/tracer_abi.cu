@@ -172,7 +172,7 @@ struct tracer_ctx {
     DevBuf<unsigned char> pres_src[2], pres_out;  // staging for host images
     uint32_t trav_cap = 0;            // tracer_set_traversal_limit: 0 = automatic
     uint32_t edge_samples = 0;        // tracer_set_edge_sampling: pieces per triangle edge, 0 = off
-    uint64_t adj_log_limit = 4ull << 30;  // tracer_set_adjoint_hit_log: bytes for pass 1's hits, 0 = none
+    uint64_t adj_log_limit = 0;       // tracer_set_adjoint_hit_log: bytes for pass 1's hits, 0 = none (pure replay)
 };
 
 namespace {

@@ -240,7 +240,8 @@ class Tracer:
         self._check(self.lib.tracer_set_edge_sampling(self.h, samples_per_edge))
 
     def set_adjoint_hit_log(self, max_bytes: int):
-        """Device memory the wavefront adjoint may keep pass 1's hits in (0 = none: pass 2 traces again)."""
+        """Device memory the wavefront adjoint may keep pass 1's hits in; 0 (the default) = none: pure
+        path replay, pass 2 traces again."""
         self._check(self.lib.tracer_set_adjoint_hit_log(self.h, max_bytes))
 
     @staticmethod
