@@ -792,13 +792,15 @@ def present_section(local: int, steps: int) -> dict:
 
 
 def gd_section(local: int, gd_steps: int, width: int, spp: int, n_tris: int, checkpoint: str | None = None,
-               every: int = 10, resume: bool = False) -> dict:
+               every: int = 10, resume: bool = False, hit_log: bool = False) -> dict:
     """c4: recover perturbed albedos by gradient descent on an L2 image loss
     (1024^2, 64 spp, depth 12, 1M triangles, 1024 materials by default).
     Each step: forward (wavefront, RGBA32F + LINEAR) and adjoint, device-timed;
     Adam on the albedo table, clamped to [1e-3, 1] (vktrace.descent).  With a
     checkpoint path the optimiser state is saved every `every` steps and at
-    the end; resume continues from that file."""
+    the end; resume continues from that file.  hit_log: the adjoint keeps
+    pass 1's hits of the current sample (tracer_set_adjoint_hit_log) instead
+    of pure path replay."""
     import numpy as np
     import torch
     from vktrace import abi, configs
@@ -806,6 +808,8 @@ def gd_section(local: int, gd_steps: int, width: int, spp: int, n_tris: int, che
     wl = configs.c4(width=width, spp=spp, n_tris=n_tris)
     tr = abi.Tracer(local)
     tr.upload_scene(wl.scene)
+    if hit_log:
+        tr.set_adjoint_hit_log(4 << 30)
     truth = wl.scene.materials.copy()
     nm = len(truth)
     p = abi.Tracer.params(wl.width, wl.height, spp=wl.spp, max_depth=wl.max_depth, rr_start=wl.rr_start,
@@ -879,7 +883,9 @@ def gd_section(local: int, gd_steps: int, width: int, spp: int, n_tris: int, che
                            "materials_with_gradient": int(seen.sum()), "materials": nm},
             "checkpoint": checkpoint,
             "peak_extra_device_memory_bytes": int(peak_extra),
-            "config": {"workload": wl.name, "optimizer": "Adam lr 0.01, albedo clamped to [1e-3, 1]"}}
+            "config": {"workload": wl.name, "optimizer": "Adam lr 0.01, albedo clamped to [1e-3, 1]",
+                       "adjoint": "hit log (pass 1's hits of the current sample kept)" if hit_log
+                       else "pure path replay (no stored path vertices)"}}
 
 
 def run_reference(args):
@@ -1122,6 +1128,8 @@ def main():
     ap.add_argument("--gd-checkpoint", default=None, help="gradient descent: .npz file for the optimiser state")
     ap.add_argument("--gd-checkpoint-every", type=int, default=10)
     ap.add_argument("--gd-resume", action="store_true", help="gradient descent: continue from --gd-checkpoint")
+    ap.add_argument("--gd-hit-log", action="store_true",
+                    help="gradient descent: the adjoint keeps pass 1's hits (tracer_set_adjoint_hit_log)")
     ap.add_argument("--present-only", action="store_true", help="time the present pass alone (--steps launches)")
     # smaller variants of the workload (profiling captures); defaults = c1
     ap.add_argument("--width", type=int, default=1920)
@@ -1136,7 +1144,7 @@ def main():
         w = args.width if args.width != 1920 else 1024
         spp = args.spp if args.spp != 16 else 64
         print(json.dumps(gd_section(dist_setup()[2], args.gd_steps, w, spp, args.gd_tris, args.gd_checkpoint,
-                                    args.gd_checkpoint_every, args.gd_resume)), flush=True)
+                                    args.gd_checkpoint_every, args.gd_resume, args.gd_hit_log)), flush=True)
     elif args.present_only:
         import torch
         torch.cuda.set_device(dist_setup()[2])
