@@ -1065,7 +1065,7 @@ def run_ours(args):
             # node fetches and the warps' SIMD efficiency, not HBM bandwidth.
             # peak/frac: against the measured HBM copy bandwidth (the common
             # denominator); l2.frac: against L2 read bandwidth, the operative one
-            "roofline": {"bound": "l1/l2 latency (scene L2-resident)", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "instruction issue (integer ALU, 68 % issue active in ncu) with L1/L2 latency behind it; scene L2-resident", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (NCU_EXTEND_DRAM_BYTES_PER_RAY * rays
                                      if kern == abi.KERNEL_WAVEFRONT else None),
