@@ -1061,11 +1061,13 @@ def run_ours(args):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 96,
                     "d2h_bytes_per_step": wl.pixels * 4},
             # the traversal's working set (4.8 MB of triangles, 2.1 MB of nodes)
-            # stays in L2: what bounds it is the latency of dependent L1/L2
-            # node fetches and the warps' SIMD efficiency, not HBM bandwidth.
+            # stays in L2: what bounds it is instruction issue (the integer
+            # pipe of the slab tests), the warps' SIMD efficiency and the
+            # latency of dependent L1/L2 node fetches, not HBM bandwidth.
             # peak/frac: against the measured HBM copy bandwidth (the common
-            # denominator); l2.frac: against L2 read bandwidth, the operative one
-            "roofline": {"bound": "instruction issue (integer ALU, 68 % issue active in ncu) with L1/L2 latency behind it; scene L2-resident", "achieved": achieved, "peak": peak,
+            # denominator); l2.frac: against L2 read bandwidth
+            "roofline": {"bound": "instruction issue (integer ALU, 68 % issue active in ncu) with L1/L2 latency "
+                                  "behind it; scene L2-resident", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (NCU_EXTEND_DRAM_BYTES_PER_RAY * rays
                                      if kern == abi.KERNEL_WAVEFRONT else None),
