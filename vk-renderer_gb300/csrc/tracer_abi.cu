@@ -1795,6 +1795,18 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         if (e == cudaSuccess) e = cudaMemcpyAsync(ab.lin.p, linear_image, npx * 16, cudaMemcpyHostToDevice, st);
         lin = ab.lin.p;
     }
+    // the boundary term's list of visible outline parts: room for 16 per edge
+    // piece on average (c3: 640k parts, 31 MB); parts beyond it are
+    // evaluated by the walk itself
+    const bool edges = d_campos && s.nt > 0 && c->edge_samples > 0;
+    uint32_t seg_cap = 0;
+    if (edges) {
+        const uint64_t cap64 = std::min<uint64_t>(16ull * s.nt * 3u * c->edge_samples, 1ull << 25);
+        seg_cap = (uint32_t)std::max<uint64_t>(cap64, 1u << 16);
+        if (e == cudaSuccess) e = dalloc(ab.segs, 3 * (size_t)seg_cap);
+        if (e == cudaSuccess) e = dalloc(ab.nsegs, 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ab.nsegs.p, 0, sizeof(uint32_t), st);
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(ab.grad.p, 0, ng * sizeof(double), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->stats.p, 0, sizeof(unsigned long long) * C_COUNT, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->status.p, 0, sizeof(int), st);
@@ -1866,16 +1878,8 @@ extern "C" int tracer_trace_adjoint(tracer_ctx* c, const tracer_frame* f, const 
         e = launch_adjoint(a, dldi, lin, ab.grad.p, s.nm, p->tie_mode, s.bvh ? 1 : 0, st);
     }
     // the camera's boundary term: triangle outlines moving across pixels
-    if (e == cudaSuccess && d_campos && s.nt > 0 && c->edge_samples > 0) {
-        // room for 16 visible parts per edge piece on average (c3: 640k parts,
-        // 31 MB); parts beyond it are evaluated by the walk itself
-        const uint64_t cap64 = std::min<uint64_t>(16ull * s.nt * 3u * c->edge_samples, 1ull << 25);
-        const uint32_t cap = (uint32_t)std::max<uint64_t>(cap64, 1u << 16);
-        e = dalloc(ab.segs, 3 * (size_t)cap);
-        if (e == cudaSuccess) e = dalloc(ab.nsegs, 1);
-        if (e == cudaSuccess) e = cudaMemsetAsync(ab.nsegs.p, 0, sizeof(uint32_t), st);
-        if (e != cudaSuccess) return cuda_fail(c, e, "boundary-term buffers");
-        EdgeArgs ea{dldi, ab.grad.p + 6 * (size_t)s.nm, {}, c->edge_samples, 0.01f, ab.segs.p, ab.nsegs.p, cap};
+    if (e == cudaSuccess && edges) {
+        EdgeArgs ea{dldi, ab.grad.p + 6 * (size_t)s.nm, {}, c->edge_samples, 0.01f, ab.segs.p, ab.nsegs.p, seg_cap};
         if (!camera_inverse(f->camera, ea.binv)) return fail(c, TRACER_ERR_INVALID_ARG, "degenerate camera basis");
         TraceArgs ae = a;
         ae.stack_depth = stack;  // the binary traversal's
